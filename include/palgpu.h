@@ -1,0 +1,140 @@
+/*
+ * palgpu.h -- C ABI of the GB300-native palinstrophy DNS step (libpalgpu.so).
+ *
+ * The reference has no FFI of its own: its "operator API" is the set of Python
+ * functions in palinstrophy/turbo_simulator.py that the sim CLI (run_dns) and
+ * the GUI facade (turbo_wrapper.py DnsSimulator) call, plus the DnsState
+ * fields they read.  Each entry point below replaces one of those functions
+ * (file:line cited beside it); palinstrophy_gb300/turbo_simulator.py binds
+ * them with ctypes and re-exports the reference's Python names.
+ *
+ * Conventions
+ *   - Every call returns an int status: PAL_OK (0) or a negative PAL_ERR_*;
+ *     pal_last_error() gives the message.  No exception crosses the ABI.
+ *   - One handle = one field on the current CUDA device, with its own stream;
+ *     a handle is used from one host thread at a time.
+ *   - Host arrays are in the reference layouts and in the handle's precision:
+ *     complex64 (interleaved float re, im) for PAL_FP32, complex128 for PAL_FP64.
+ *       om2, fnm1 : (N, N/2)     [z][kx]
+ *       uc_low    : (2, N, N/2)  [comp][z][kx]  (uc_full[0:2, :N, :N/2])
+ *       ur planes : (M, M) real  [z][x], M = 3N/2
+ *   - Step calls are asynchronous on the handle's stream; only pal_get_* ,
+ *     pal_compute_cflm, pal_diagnostics and pal_synchronize wait for it.
+ */
+#ifndef PALGPU_H
+#define PALGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PAL_OK = 0,
+  PAL_ERR_INVALID = -1,     /* bad argument (null handle/pointer, unsupported N, ...) */
+  PAL_ERR_CUDA = -2,        /* a CUDA runtime call failed */
+  PAL_ERR_OOM = -3,         /* device allocation failed */
+  PAL_ERR_STATE = -4,       /* call out of order (e.g. step3 before step2b) */
+  PAL_ERR_NONFINITE = -5    /* NaN/Inf detected in the field */
+};
+
+enum { PAL_FP32 = 0, PAL_FP64 = 1 };
+enum { PAL_CNAB2 = 0, PAL_LS_IMEX_RK3 = 1 };
+enum { PAL_FIELD_OM2 = 0, PAL_FIELD_FNM1 = 1, PAL_FIELD_UR_U = 2, PAL_FIELD_UR_V = 3 };
+enum { PAL_SPEC_KM3 = 0, PAL_SPEC_PAO = 1 };
+enum { PAL_SC_T = 0, PAL_SC_DT = 1, PAL_SC_CN = 2, PAL_SC_CNM1 = 3, PAL_SC_VISC = 4, PAL_SC_CFLNUM = 5, PAL_SC_IT = 6 };
+
+typedef struct pal_handle pal_handle;
+
+/* Diagnostics, all FP64 (turbo_simulator.py:764-810, turbo_main.py:1947-1959, 2015-2073). */
+typedef struct pal_diag {
+  double U;                  /* sqrt(mean(u^2 + v^2)) on the 3/2 grid */
+  double L;                  /* 2 pi sum(w |om|^2/K^3) / E */
+  double tau_l;              /* L / U */
+  double E;                  /* sum over K2>0 of w |om|^2 / K2 */
+  double Z;                  /* enstrophy sum: sum w |om|^2 - |om_00|^2 */
+  double P;                  /* palinstrophy sum: sum w K2 |om|^2 */
+  double kmax2;              /* max K2 of the compact band */
+  double pal_over_ens_kmax2; /* P / (Z kmax2), the GUI metric */
+  double cflm;               /* max(|u|+|v|) N/(2 pi) */
+  double energy_joules;      /* 0.5 (2 pi)^2 mean(u^2+v^2) */
+  int nonfinite;             /* 1 if a NaN/Inf was seen */
+} pal_diag;
+
+/* create_dns_state (turbo_simulator.py:878-1054): allocate the device state for
+ * an N x N field (N in 32..8192, see pal_supported).  visc defaults to
+ * float32(1/Re) as dns_pao_host_init sets it (turbo_simulator.py:470, 1139);
+ * cfl is the CFL target cflnum.  The state is empty until pal_set_* calls. */
+int pal_create(int N, int precision, double Re, double cfl, pal_handle** out);
+int pal_destroy(pal_handle* h);
+/* 1 if (N, precision) has compiled kernels, else 0. */
+int pal_supported(int N, int precision);
+/* Device properties of the handle's GPU: SM count and max dynamic smem per block. */
+int pal_device_info(int* sm_count, int* smem_optin, char* name, size_t name_len);
+
+/* Initial state as create_dns_state leaves it (turbo_simulator.py:1191-1234):
+ * om2 and fnm1 (fnm1 may be NULL for zeros), and the velocity low band that
+ * the first dns_step2a transforms (uc_low may be NULL: then the velocity is
+ * rebuilt from om2 by the inversion of turbo_simulator.py:1555-1585). */
+int pal_set_spectral_state(pal_handle* h, const void* om2, const void* fnm1);
+int pal_set_velocity_spectrum(pal_handle* h, const void* uc_low);
+
+/* DnsState scalar mirror (turbo_simulator.py:742-753, 846-854). */
+int pal_set_scalars(pal_handle* h, double t, double dt, double cn, double cnm1, double visc,
+                    double cflnum, long long it);
+int pal_get_scalars(pal_handle* h, double* t, double* dt, double* cn, double* cnm1, double* visc,
+                    double* cflnum, long long* it);
+/* One scalar (PAL_SC_*), as DnsState.__setattr__ mirrors dt/cn/cnm1 into the
+ * device time_scalars (turbo_simulator.py:742-753); stream-ordered. */
+int pal_set_scalar(pal_handle* h, int which, double value);
+
+/* dns_step2a (turbo_simulator.py:1949-2100): pad + inverse transform of the
+ * velocity spectrum.  After pal_step3 the column half is already done by the
+ * fused column kernel, so this only completes a pending initial transform. */
+int pal_step2a(pal_handle* h);
+/* dns_step2b (turbo_simulator.py:1378-1513): products + forward transform
+ * (the x half; the z half is fused into pal_step3). */
+int pal_step2b(pal_handle* h);
+/* dns_step3 (turbo_simulator.py:1588-1771): nonlinear term, CNAB2 update,
+ * fnm1 <- fn, cnm1 <- cn, omega -> velocity inversion (+ the z half of the next
+ * dns_step2a). */
+int pal_step3(pal_handle* h);
+/* dns_step_ls_imex_rk3 (turbo_simulator.py:1900-1943): one full 3-stage step. */
+int pal_step_rk3(pal_handle* h);
+/* The run_dns hot loop (turbo_simulator.py:2831-2848) for nsteps steps of
+ * `method`: after the step with iteration number it (counted by the handle),
+ * NEXTDT runs if update > 0 and (it % update == 0 || it == 1 || (final_update
+ * && last step of this call)); t += dt_old and it += 1 every step. */
+int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update);
+
+/* compute_cflm (turbo_simulator.py:2106-2125), waits for the result. */
+int pal_compute_cflm(pal_handle* h, double* cflm);
+/* next_dt (turbo_simulator.py:2127-2167): CFLM, cn = 0.8 + 0.2 cflnum/CFL,
+ * dt *= cn on the device.  With sync_host != 0 it waits and stores CFLM. */
+int pal_next_dt(pal_handle* h, int sync_host, double* cflm);
+/* flow_eddy_metrics + the GUI sums in one pass; waits. */
+int pal_diagnostics(pal_handle* h, pal_diag* out);
+
+/* Copy a field to host memory in the reference layout (waits). */
+int pal_get_field(pal_handle* h, int which, void* host_dst);
+/* Device pointer of a field: om2/fnm1 are stored transposed, [kx][z] (N/2 x N);
+ * the physical planes [z][x] are valid after pal_get_field(UR_U/UR_V) or
+ * pal_materialize_physical. */
+int pal_field_device_ptr(pal_handle* h, int which, void** ptr);
+int pal_materialize_physical(pal_handle* h);
+int pal_synchronize(pal_handle* h);
+/* The handle's CUDA stream (cudaStream_t), for event timing or interop. */
+int pal_get_stream(pal_handle* h, void** stream);
+int pal_last_error(pal_handle* h, char* buf, size_t n);
+
+/* Host-side PAO / KM3 initial condition (turbo_simulator.py:213-485, 1059-1239,
+ * 1314-1361), complex64 outputs: om2 (N, N/2) and uc_low (2, N, N/2).
+ * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed. */
+int pal_pao_generate(int N, double K0, double Re, int seed, int spectrum, void* om2, void* uc_low,
+                     double* stats, int* seed_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PALGPU_H */

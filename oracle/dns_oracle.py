@@ -1,0 +1,322 @@
+"""CPU oracle for the palinstrophy pseudo-spectral DNS step.
+
+TEST INFRASTRUCTURE ONLY.  ``palinstrophy_gb300`` never imports this module.
+It is used by ``tests/`` (parity checker), ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py``.
+
+It restates the reference CPU (NumPy + scipy.fft) path of
+``palinstrophy/turbo_simulator.py``, operation for operation:
+
+  step2a   dealias pad + inverse irfft2(norm='forward')   turbo_simulator.py:2020-2034, 1246-1262
+  step2b   uu, ww, uw products, rfft2, zero row z=N       turbo_simulator.py:1449-1513, 1276-1297
+  step3    gathered nonlinear term, CNAB2, fnm1, inversion turbo_simulator.py:1520-1585, 1731-1771
+  rk3      LS-IMEX-RK3 (alpha, beta) stages              turbo_simulator.py:1900-1943
+  cflm     max(|u|+|w|) * N/(2 pi)                        turbo_simulator.py:2106-2125
+  next_dt  cn = 0.8 + 0.2 cflnum/CFL, dt *= cn            turbo_simulator.py:2127-2167
+  driver   run_dns cadence (it=1, it%UPDATE==0, it=STEPS) turbo_simulator.py:2810-2848
+  metrics  flow_eddy_metrics, pal_over_ens_kmax2,         turbo_simulator.py:764-810,
+           energy_joules, omega-spectrum shell bins       turbo_main.py:1947-1959, 2015-2073,
+                                                          turbo_simulator.py:2317-2383
+
+``dtype=np.float64`` is the FP64 oracle (complex128 everywhere, constants in
+double).  ``dtype=np.float32`` keeps the reference's float32 casts and
+operation order, so that on one machine it reproduces the reference CPU path
+bit for bit; it is also the timed CPU baseline ("port").
+
+Arrays use the reference layouts: om2/fnm1 (N, N/2) [z, kx];
+uc_full (3, M, M/2+1) [comp, z, kx]; ur_full (3, M, M) [comp, z, x], M = 3N/2.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import scipy.fft as spfft
+
+RK3_ALPHA = (8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0)
+RK3_BETA = (0.0, -17.0 / 60.0, -5.0 / 12.0)
+
+
+class OracleState:
+    """Minimal DnsState twin holding the arrays and scalars one step touches."""
+
+    def __init__(self, N, om2, uc_low, visc, cflnum, dtype=np.float64, workers=None):
+        if N % 4:
+            raise ValueError("N must be a multiple of 4")
+        self.rdt = np.dtype(dtype)
+        self.cdt = np.dtype(np.complex64 if self.rdt == np.float32 else np.complex128)
+        self.f32 = self.rdt == np.float32
+        self.N = N
+        self.Nh = N // 2
+        self.M = 3 * N // 2
+        self.NK_full = self.M // 2 + 1
+        # pocketfft batches lines differently per worker count; the reference
+        # passes min(8, cpu_count) (turbo_simulator.py:912), so the FP32 port
+        # is bit-exact with it only at that same count.
+        self.workers = workers if workers else min(8, os.cpu_count() or 1)
+        M, Nh = self.M, self.Nh
+        self.ur_full = np.zeros((3, M, M), self.rdt)
+        self.uc_full = np.zeros((3, M, self.NK_full), self.cdt)
+        self.uc_full[0:2, :N, :Nh] = np.asarray(uc_low).astype(self.cdt)
+        self.om2 = np.asarray(om2).astype(self.cdt).copy()
+        self.fnm1 = np.zeros_like(self.om2)
+        self.visc = float(visc)
+        self.cflnum = float(cflnum)
+        self.t = 0.0
+        self.dt = 0.0
+        self.cn = 1.0
+        self.cnm1 = 0.0
+        self.it = 0
+        r = self.rdt.type
+        alfa = np.arange(Nh, dtype=self.rdt)
+        kz = np.arange(N)
+        gamma = np.where(kz < Nh, kz, kz - N).astype(self.rdt)
+        self.alfa, self.gamma = alfa, gamma
+        ax = alfa[None, :]
+        gz = gamma[:, None]
+        self.K2 = (ax * ax + gz * gz).astype(self.rdt)
+        self.GA = (gz * ax).astype(self.rdt)
+        self.G2mA2 = (gz * gz - ax * ax).astype(self.rdt)
+        self.invK2_sub = (r(1.0) / (self.K2[:, 1:] + r(1.0e-30))).astype(self.rdt)
+        mask0 = (kz >= 1) & (np.abs(gamma) > 0.0)
+        safe = np.where(mask0, gamma, r(1.0))
+        self.inv_gamma0 = (r(1.0) / safe).astype(self.rdt) * mask0.astype(self.rdt)
+        m32 = r(1.5) * r(N)
+        self.divxz = r(1.0) / (m32 * m32)
+        self.inv_dx = float(N) / (2.0 * math.pi)
+
+    # ---------------- scalar helpers ---------------------------------
+    def _s(self, v):
+        """Scalar in the working precision (float32 cast as in TS:1736-1737)."""
+        return self.rdt.type(v)
+
+
+def step2a(S: OracleState) -> None:
+    """Pad the velocity low band to the 3/2 grid and inverse-transform (TS:2020-2034)."""
+    N, Nh = S.N, S.Nh
+    UC = S.uc_full
+    hi_end = min(3 * N // 4, S.NK_full - 1)
+    UC[0:2, :, Nh:hi_end + 1] = 0
+    UC[0:2, N:N + Nh, :Nh] = UC[0:2, Nh:N, :Nh]
+    UC[0:2, Nh:N, :Nh] = 0
+    ur01 = spfft.irfft2(UC[0:2], axes=(1, 2), overwrite_x=True,
+                        workers=S.workers, norm="forward")
+    S.ur_full[0:2] = ur01
+
+
+def step2b(S: OracleState) -> None:
+    """In-place products, forward rfft2 of the 3 planes, zero row z=N (TS:1449-1513)."""
+    UR = S.ur_full
+    u, w = UR[0], UR[1]
+    np.multiply(u, w, out=UR[2])
+    np.multiply(u, u, out=UR[0])
+    np.multiply(w, w, out=UR[1])
+    S.uc_full[...] = spfft.rfft2(UR, axes=(1, 2), overwrite_x=True, workers=S.workers)
+    S.uc_full[0:3, S.N, 0:S.Nh] = 0
+
+
+def nonlinear(S: OracleState) -> np.ndarray:
+    """fn = divxz [GA (F uu - F ww) + (G^2 - A^2) F uw] at gathered rows (TS:1520-1552)."""
+    N, Nh = S.N, S.Nh
+    low = S.uc_full[:, :, :Nh]
+    g = np.concatenate([low[:, :Nh], low[:, N:N + Nh]], axis=1)  # (3, N, Nh)
+    out = np.subtract(g[0], g[1])
+    np.multiply(out, S.GA, out=out)
+    tmp = np.multiply(g[2], S.G2mA2)
+    np.add(out, tmp, out=out)
+    np.multiply(out, S.divxz, out=out)
+    return out
+
+
+def reconstruct_velocity(S: OracleState) -> None:
+    """omega -> (u1, u3) low band of uc_full (TS:1555-1585)."""
+    N, Nh = S.N, S.Nh
+    om = S.om2
+    out1 = np.zeros_like(om)
+    out2 = np.zeros_like(om)
+    mi = S.cdt.type(-1j)
+    pi_ = S.cdt.type(1j)
+    if Nh > 1:
+        o1 = om[:, 1:] * S.invK2_sub
+        o1 = o1 * S.gamma[:, None]
+        out1[:, 1:] = o1 * mi
+        o2 = om[:, 1:] * S.invK2_sub
+        o2 = o2 * S.alfa[1:][None, :]
+        out2[:, 1:] = o2 * pi_
+    out1[:, 0] = mi * om[:, 0] * S.inv_gamma0
+    out2[:, 0] = 0
+    S.uc_full[0, :N, :Nh] = out1
+    S.uc_full[1, :N, :Nh] = out2
+
+
+def step3(S: OracleState) -> None:
+    """CNAB2 update with the stale-cn AB2 weights (TS:1731-1771)."""
+    s = S._s
+    visc, dt, cnm1 = s(S.visc), s(S.dt), s(S.cnm1)
+    fn = nonlinear(S)
+    vt = s(0.5) * visc * dt
+    arg = S.K2 * vt
+    den = arg + s(1.0)
+    c2 = s(0.5) * dt * (s(2.0) + cnm1)
+    c3 = -s(0.5) * dt * cnm1
+    num = S.om2 - S.om2 * arg
+    num = num + fn * c2
+    num = num + S.fnm1 * c3
+    S.om2 = (num / den).astype(S.cdt)
+    S.fnm1 = fn
+    reconstruct_velocity(S)
+    S.cnm1 = float(S.cn)
+
+
+def rk3(S: OracleState) -> None:
+    """One LS-IMEX-RK3 step: 3 x (step2b, stage update, step2a) (TS:1900-1943)."""
+    s = S._s
+    dt, visc = s(S.dt), s(S.visc)
+    for a_, b_ in zip(RK3_ALPHA, RK3_BETA):
+        a, b = s(a_), s(b_)
+        step2b(S)
+        fn = nonlinear(S)
+        rhs = s(1.0) - S.K2 * (b * dt * visc)
+        num = S.om2 * rhs
+        num = num + fn * (a * dt)
+        num = num + S.fnm1 * (b * dt)
+        den = S.K2 * (a * dt * visc) + s(1.0)
+        S.om2 = (num / den).astype(S.cdt)
+        S.fnm1 = fn
+        reconstruct_velocity(S)
+        step2a(S)
+
+
+def cnab2(S: OracleState) -> None:
+    step2b(S)
+    step3(S)
+    step2a(S)
+
+
+def compute_cflm(S: OracleState) -> float:
+    """max(|u|+|w|) * N/(2 pi) over the 3/2 grid (TS:2106-2125)."""
+    tmp = np.abs(S.ur_full[0]) + np.abs(S.ur_full[1])
+    return float(tmp.max() * S.inv_dx)
+
+
+def next_dt(S: OracleState) -> float:
+    """CFL-adaptive dt update in double (TS:2160-2167)."""
+    cflm = compute_cflm(S)
+    if cflm <= 0.0 or S.dt <= 0.0:
+        return cflm
+    cfl = cflm * S.dt * math.pi
+    S.cn = 0.8 + 0.2 * (S.cflnum / cfl)
+    S.dt = S.dt * S.cn
+    return cflm
+
+
+def init_dt(S: OracleState) -> float:
+    """Initial step2a + dt = cflnum/(CFLM pi), cn=1, cnm1=0 (TS:2810-2823)."""
+    step2a(S)
+    cflm = compute_cflm(S)
+    S.dt = S.cflnum / (cflm * math.pi)
+    S.cn, S.cnm1, S.t = 1.0, 0.0, 0.0
+    return cflm
+
+
+def run(S: OracleState, steps: int, method: str = "CNAB2", update: int = 100,
+        dt_replay=None, log=None) -> None:
+    """The run_dns hot loop (TS:2831-2848).
+
+    ``dt_replay``: optional sequence of (dt, cn) pairs, one per next_dt call, that
+    replaces the computed values (the reference's dt sequence replayed).
+    ``log``: optional list receiving (it, t, dt, cn, cflm) at each next_dt.
+    """
+    step = rk3 if method.upper() == "LS_IMEX_RK3" else cnab2
+    nd = 0
+    for it in range(1, steps + 1):
+        S.it = it
+        dt_old = S.dt
+        step(S)
+        if it % update == 0 or it == 1 or it == steps:
+            cflm = next_dt(S)
+            if dt_replay is not None:
+                S.dt, S.cn = float(dt_replay[nd][0]), float(dt_replay[nd][1])
+            nd += 1
+            if log is not None:
+                log.append((it, S.t, S.dt, S.cn, cflm))
+        S.t += dt_old
+
+
+# ---------------- diagnostics ---------------------------------------
+def rfft_weights(nh: int, last_one: bool = True) -> np.ndarray:
+    """[1,2,...,2,1] as the eddy/pal metrics use it (TS:778-781, TM:2040-2044)."""
+    w = np.full(nh, 2.0)
+    w[0] = 1.0
+    if last_one and nh > 1:
+        w[-1] = 1.0
+    return w
+
+
+def flow_eddy_metrics(S: OracleState):
+    """(U, L, tau_L) in double from ur_full and om2 (TS:764-810)."""
+    u, v = S.ur_full[0].astype(np.float64), S.ur_full[1].astype(np.float64)
+    U = math.sqrt(max(0.0, float(np.mean(u * u + v * v))))
+    K2 = S.K2.astype(np.float64)
+    p = np.abs(S.om2.astype(np.complex128)) ** 2
+    power = np.where(K2 > 0, p / np.where(K2 > 0, K2, 1.0), 0.0)
+    wp = power * rfft_weights(S.Nh)[None, :]
+    e = float(wp.sum() - wp[0, 0])
+    if e <= 0.0:
+        return U, float("nan"), float("nan")
+    invk = np.where(K2 > 0, 1.0 / np.sqrt(np.where(K2 > 0, K2, 1.0)), 0.0)
+    L = 2.0 * math.pi * float((wp * invk).sum()) / e
+    return U, L, (L / U if U > 0 else float("nan"))
+
+
+def spectral_sums(S: OracleState) -> dict:
+    """E, Z (enstrophy), P (palinstrophy), kmax^2 and the GUI ratio (TM:2015-2073)."""
+    K2 = S.K2.astype(np.float64)
+    p = np.abs(S.om2.astype(np.complex128)) ** 2
+    w = rfft_weights(S.Nh)[None, :]
+    wp = w * p
+    Z = float(wp.sum() - p[0, 0])
+    kmax2 = float(K2.max())
+    P = float((w * K2 * p).sum())
+    power = np.where(K2 > 0, p / np.where(K2 > 0, K2, 1.0), 0.0)
+    E = float((power * w).sum())
+    ratio = P / (Z * kmax2) if Z > 0 and kmax2 > 0 else 0.0
+    return {"E": E, "Z": Z, "P": P, "kmax2": kmax2, "pal_over_ens_kmax2": ratio}
+
+
+def energy_joules(S: OracleState) -> float:
+    """0.5 (2 pi)^2 <u^2+v^2> on the 3/2 grid (TM:1947-1959)."""
+    u, v = S.ur_full[0].astype(np.float64), S.ur_full[1].astype(np.float64)
+    return 0.5 * (2.0 * math.pi) ** 2 * float((u * u).sum() + (v * v).sum()) / u.size
+
+
+def omega_spectrum_bins(S: OracleState):
+    """Shell sums of |omega|^2/k^2 (weight 2 for kx>0) -- TS:2317-2383."""
+    n = S.N
+    nbins = max(32, 2 * n)
+    r_max = math.sqrt(2.0)
+    k_nyq = 0.5 * n
+    scale2 = float(S.M * S.M) ** 2
+    om = S.om2.astype(np.complex128)
+    kx = np.arange(S.Nh, dtype=np.float64)
+    wt = np.ones(S.Nh)
+    wt[1:] = 2.0
+    esum = np.zeros(nbins)
+    cnt = np.zeros(nbins, dtype=np.int64)
+    for z in range(n):
+        kz = z if z < n // 2 else z - n
+        k2 = kx * kx + float(kz * kz)
+        m = k2 > 0
+        b = np.floor((np.sqrt(k2[m]) / k_nyq / r_max) * nbins).astype(np.int64)
+        np.clip(b, 0, nbins - 1, out=b)
+        p = (om[z, m].real ** 2 + om[z, m].imag ** 2) / k2[m]
+        esum += np.bincount(b, weights=p * wt[m] * scale2, minlength=nbins)
+        cnt += np.bincount(b, weights=wt[m], minlength=nbins).astype(np.int64)
+    return esum, cnt
+
+
+def rel_l2(ref, cand) -> float:
+    ref = np.asarray(ref).astype(np.complex128)
+    cand = np.asarray(cand).astype(np.complex128)
+    return float(np.linalg.norm((cand - ref).ravel()) / max(np.linalg.norm(ref.ravel()), 1e-300))

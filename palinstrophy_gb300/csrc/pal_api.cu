@@ -1,0 +1,521 @@
+// C ABI of libpalgpu.so: handle-owned device state, stream-ordered launches of
+// the fused row/column kernels, and the reference-shaped entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "palgpu.h"
+#include "pal_launch.cuh"
+
+using pal::DevScalars;
+using pal::KernelSet;
+using pal::StepArgs;
+
+namespace {
+
+enum State { ST_EMPTY = 0, ST_VEL_PENDING = 1, ST_U = 2, ST_P = 3 };
+
+// LS-IMEX-RK3 coefficients (turbo_simulator.py:1902-1903)
+constexpr double kRkAlpha[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+constexpr double kRkBeta[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
+
+thread_local std::string g_err;
+
+}  // namespace
+
+struct pal_handle {
+  int N = 0, M = 0, Nh = 0, precision = 0;
+  size_t esz = 0;  // bytes per complex element
+  const KernelSet* ks = nullptr;
+  cudaStream_t stream = nullptr;
+  void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr, *tw = nullptr;
+  void *stage = nullptr, *phys = nullptr;
+  DevScalars* sc = nullptr;
+  DevScalars* sc_host = nullptr;  // pinned mirror
+  double* part = nullptr;
+  int state = ST_EMPTY;
+  bool vel_uploaded = false;  // ST_VEL_PENDING source: stage buffer (true) or om inversion
+  long long it = 0;           // host copy of the iteration counter
+  int spectral_blocks = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(pal_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(pal_handle* h, cudaError_t e, const char* what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? PAL_ERR_OOM : PAL_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PAL_CK(h, expr)                                   \
+  do {                                                    \
+    cudaError_t e_ = (expr);                              \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr); \
+  } while (0)
+
+#define PAL_LAUNCHED(h, what)                                  \
+  do {                                                         \
+    cudaError_t e_ = cudaGetLastError();                       \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, (what));  \
+  } while (0)
+
+StepArgs base_args(pal_handle* h) {
+  StepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.w0 = h->w0;
+  a.w1 = h->w1;
+  a.om = h->om;
+  a.fnm1 = h->fnm1;
+  a.tw = h->tw;
+  a.sc = h->sc;
+  a.part = h->part;
+  a.phys = h->phys;
+  a.N = h->N;
+  return a;
+}
+
+// Forward twiddles exp(-2 pi i m / M), evaluated in extended precision and
+// rounded once to the working precision.
+void make_twiddles(int M, int precision, void* host) {
+  for (int m = 0; m < M; ++m) {
+    const long double ang = 2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)M;
+    const double c = (double)cosl(ang), s = (double)-sinl(ang);
+    if (precision == PAL_FP64) {
+      static_cast<double*>(host)[2 * m] = c;
+      static_cast<double*>(host)[2 * m + 1] = s;
+    } else {
+      static_cast<float*>(host)[2 * m] = (float)c;
+      static_cast<float*>(host)[2 * m + 1] = (float)s;
+    }
+  }
+}
+
+int resolve_velocity(pal_handle* h) {
+  if (h->state == ST_EMPTY) return fail(h, PAL_ERR_STATE, "no spectral state set");
+  if (h->state != ST_VEL_PENDING) return PAL_OK;
+  StepArgs a = base_args(h);
+  a.src = h->vel_uploaded ? h->stage : nullptr;
+  h->ks->col_inv(a, h->stream);
+  PAL_LAUNCHED(h, "k_col_inv");
+  h->state = ST_U;
+  h->vel_uploaded = false;
+  return PAL_OK;
+}
+
+int launch_row(pal_handle* h, int flags) {
+  StepArgs a = base_args(h);
+  a.flags = flags;
+  h->ks->row(a, h->stream);
+  PAL_LAUNCHED(h, "k_row");
+  h->state = ST_P;
+  return PAL_OK;
+}
+
+int launch_col(pal_handle* h, int scheme, int stage, int flags) {
+  StepArgs a = base_args(h);
+  a.flags = flags;
+  a.scheme = scheme;
+  if (scheme == 1) {
+    a.alpha = kRkAlpha[stage];
+    a.beta = kRkBeta[stage];
+  }
+  h->ks->col(a, h->stream);
+  PAL_LAUNCHED(h, "k_col");
+  h->state = ST_U;
+  return PAL_OK;
+}
+
+int launch_phys(pal_handle* h, int flags) {
+  int rc = resolve_velocity(h);
+  if (rc) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "physical field requested between step2b and step3");
+  StepArgs a = base_args(h);
+  a.flags = flags | pal::F_STATS;
+  h->ks->phys(a, h->stream);
+  PAL_LAUNCHED(h, "k_phys");
+  return PAL_OK;
+}
+
+int read_scalars(pal_handle* h) {
+  PAL_CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+// One full step; the first row pass carries a deferred NEXTDT when `dt_update`.
+int one_step(pal_handle* h, int method, bool dt_update, bool advance) {
+  const int rflags = dt_update ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
+  int rc;
+  if (method == PAL_CNAB2) {
+    if ((rc = launch_row(h, rflags))) return rc;
+    return launch_col(h, 0, 0, pal::F_CNM1 | (advance ? pal::F_ADVANCE : 0));
+  }
+  for (int s = 0; s < 3; ++s) {
+    if ((rc = launch_row(h, s == 0 ? rflags : 0))) return rc;
+    if ((rc = launch_col(h, 1, s, (s == 2 && advance) ? pal::F_ADVANCE : 0))) return rc;
+  }
+  return PAL_OK;
+}
+
+int check(pal_handle* h) {
+  if (!h) return fail(nullptr, PAL_ERR_INVALID, "null handle");
+  return PAL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pal_supported(int N, int precision) {
+  if (precision == PAL_FP32) return pal_kernels_f32(N) != nullptr;
+  if (precision == PAL_FP64) return pal_kernels_f64(N) != nullptr;
+  return 0;
+}
+
+int pal_device_info(int* sm_count, int* smem_optin, char* name, size_t name_len) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+  cudaDeviceProp p;
+  e = cudaGetDeviceProperties(&p, dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceProperties");
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  if (smem_optin) *smem_optin = (int)p.sharedMemPerBlockOptin;
+  if (name && name_len) {
+    std::strncpy(name, p.name, name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  return PAL_OK;
+}
+
+int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
+  if (!out) return fail(nullptr, PAL_ERR_INVALID, "out is null");
+  *out = nullptr;
+  if (precision != PAL_FP32 && precision != PAL_FP64) return fail(nullptr, PAL_ERR_INVALID, "precision must be PAL_FP32 or PAL_FP64");
+  const KernelSet* ks = precision == PAL_FP32 ? pal_kernels_f32(N) : pal_kernels_f64(N);
+  if (!ks) return fail(nullptr, PAL_ERR_INVALID, "unsupported grid N=" + std::to_string(N) + " for this precision");
+  if (!(Re > 0.0) || !(cfl > 0.0)) return fail(nullptr, PAL_ERR_INVALID, "Re and cfl must be positive");
+  pal_handle* h = new pal_handle();
+  h->N = N;
+  h->M = 3 * N / 2;
+  h->Nh = N / 2;
+  h->precision = precision;
+  h->esz = precision == PAL_FP32 ? 8 : 16;
+  h->ks = ks;
+  auto bail = [&](int code) {
+    pal_destroy(h);
+    return code;
+  };
+  cudaError_t e = ks->configure();
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "kernel configure"));
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaStreamCreate"));
+  const size_t plane_w = (size_t)h->Nh * h->M * h->esz;
+  const size_t plane_om = (size_t)h->Nh * N * h->esz;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  h->spectral_blocks = std::max(1, std::min(4 * sms, (int)(((size_t)N * h->Nh + 255) / 256)));
+  const size_t part_n = (size_t)std::max(h->M, std::max(1024, h->spectral_blocks)) * 5;
+  void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw};
+  const size_t sizes[] = {plane_w, plane_w, plane_om, plane_om, 2 * plane_om, (size_t)h->M * h->esz};
+  for (int i = 0; i < 6; ++i) {
+    e = cudaMalloc(bufs[i], sizes[i]);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc state"));
+    e = cudaMemsetAsync(*bufs[i], 0, sizes[i], h->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemset state"));
+  }
+  e = cudaMalloc(&h->sc, sizeof(DevScalars));
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc scalars"));
+  e = cudaMalloc(&h->part, part_n * sizeof(double));
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc partials"));
+  e = cudaMallocHost(&h->sc_host, sizeof(DevScalars));
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMallocHost"));
+  std::memset(h->sc_host, 0, sizeof(DevScalars));
+  h->sc_host->cn = 1.0;
+  h->sc_host->visc = (double)(float)(1.0 / (double)(float)Re);
+  h->sc_host->cflnum = cfl;
+  e = cudaMemcpyAsync(h->sc, h->sc_host, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "upload scalars"));
+  {
+    std::string tw((size_t)h->M * h->esz, '\0');
+    make_twiddles(h->M, precision, &tw[0]);
+    e = cudaMemcpyAsync(h->tw, tw.data(), tw.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "upload twiddles"));
+  }
+  *out = h;
+  return PAL_OK;
+}
+
+int pal_destroy(pal_handle* h) {
+  if (!h) return PAL_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* bufs[] = {h->w0, h->w1, h->om, h->fnm1, h->stage, h->tw, h->phys, h->sc, h->part};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (h->sc_host) cudaFreeHost(h->sc_host);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PAL_OK;
+}
+
+int pal_set_spectral_state(pal_handle* h, const void* om2, const void* fnm1) {
+  if (int rc = check(h)) return rc;
+  if (!om2) return fail(h, PAL_ERR_INVALID, "om2 is null");
+  const size_t bytes = (size_t)h->N * h->Nh * h->esz;
+  PAL_CK(h, cudaMemcpyAsync(h->stage, om2, bytes, cudaMemcpyHostToDevice, h->stream));
+  h->ks->transpose(h->stage, h->om, h->N, h->Nh, 1, h->stream);
+  PAL_LAUNCHED(h, "transpose om2");
+  if (fnm1) {
+    PAL_CK(h, cudaMemcpyAsync(h->stage, fnm1, bytes, cudaMemcpyHostToDevice, h->stream));
+    h->ks->transpose(h->stage, h->fnm1, h->N, h->Nh, 1, h->stream);
+    PAL_LAUNCHED(h, "transpose fnm1");
+  } else {
+    PAL_CK(h, cudaMemsetAsync(h->fnm1, 0, bytes, h->stream));
+  }
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  h->state = ST_VEL_PENDING;
+  h->vel_uploaded = false;
+  return PAL_OK;
+}
+
+int pal_set_velocity_spectrum(pal_handle* h, const void* uc_low) {
+  if (int rc = check(h)) return rc;
+  if (h->state == ST_EMPTY) return fail(h, PAL_ERR_STATE, "set the spectral state first");
+  if (!uc_low) {
+    h->state = ST_VEL_PENDING;
+    h->vel_uploaded = false;
+    return PAL_OK;
+  }
+  const size_t bytes = 2 * (size_t)h->N * h->Nh * h->esz;
+  PAL_CK(h, cudaMemcpyAsync(h->stage, uc_low, bytes, cudaMemcpyHostToDevice, h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  h->state = ST_VEL_PENDING;
+  h->vel_uploaded = true;
+  return PAL_OK;
+}
+
+int pal_set_scalars(pal_handle* h, double t, double dt, double cn, double cnm1, double visc, double cflnum,
+                    long long it) {
+  if (int rc = check(h)) return rc;
+  PAL_CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  DevScalars* s = h->sc_host;
+  s->t = t;
+  s->dt = dt;
+  s->cn = cn;
+  s->cnm1 = cnm1;
+  s->visc = visc;
+  s->cflnum = cflnum;
+  s->it = it;
+  h->it = it;
+  PAL_CK(h, cudaMemcpyAsync(h->sc, h->sc_host, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+int pal_set_scalar(pal_handle* h, int which, double value) {
+  if (int rc = check(h)) return rc;
+  size_t off;
+  switch (which) {
+    case PAL_SC_T: off = offsetof(DevScalars, t); break;
+    case PAL_SC_DT: off = offsetof(DevScalars, dt); break;
+    case PAL_SC_CN: off = offsetof(DevScalars, cn); break;
+    case PAL_SC_CNM1: off = offsetof(DevScalars, cnm1); break;
+    case PAL_SC_VISC: off = offsetof(DevScalars, visc); break;
+    case PAL_SC_CFLNUM: off = offsetof(DevScalars, cflnum); break;
+    case PAL_SC_IT: {
+      const long long it = (long long)value;
+      h->it = it;
+      PAL_CK(h, cudaMemcpyAsync(reinterpret_cast<char*>(h->sc) + offsetof(DevScalars, it), &it, sizeof(it),
+                                cudaMemcpyHostToDevice, h->stream));
+      PAL_CK(h, cudaStreamSynchronize(h->stream));
+      return PAL_OK;
+    }
+    default: return fail(h, PAL_ERR_INVALID, "unknown scalar");
+  }
+  PAL_CK(h, cudaMemcpyAsync(reinterpret_cast<char*>(h->sc) + off, &value, sizeof(double), cudaMemcpyHostToDevice,
+                            h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+int pal_get_scalars(pal_handle* h, double* t, double* dt, double* cn, double* cnm1, double* visc, double* cflnum,
+                    long long* it) {
+  if (int rc = check(h)) return rc;
+  if (int rc = read_scalars(h)) return rc;
+  const DevScalars* s = h->sc_host;
+  if (t) *t = s->t;
+  if (dt) *dt = s->dt;
+  if (cn) *cn = s->cn;
+  if (cnm1) *cnm1 = s->cnm1;
+  if (visc) *visc = s->visc;
+  if (cflnum) *cflnum = s->cflnum;
+  if (it) *it = s->it;
+  return PAL_OK;
+}
+
+int pal_step2a(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  if (h->state == ST_P) return fail(h, PAL_ERR_STATE, "dns_step2a after dns_step2b without dns_step3");
+  return resolve_velocity(h);
+}
+
+int pal_step2b(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "dns_step2b needs the physical velocity (call dns_step2a)");
+  return launch_row(h, 0);
+}
+
+int pal_step3(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  if (h->state != ST_P) return fail(h, PAL_ERR_STATE, "dns_step3 needs the products of dns_step2b");
+  return launch_col(h, 0, 0, pal::F_CNM1);
+}
+
+int pal_step_rk3(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "LS-IMEX-RK3 step needs the physical velocity");
+  return one_step(h, PAL_LS_IMEX_RK3, false, false);
+}
+
+int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update) {
+  if (int rc = check(h)) return rc;
+  if (method != PAL_CNAB2 && method != PAL_LS_IMEX_RK3) return fail(h, PAL_ERR_INVALID, "unknown time stepper");
+  if (nsteps < 0) return fail(h, PAL_ERR_INVALID, "nsteps < 0");
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "pal_step needs the physical velocity");
+  bool pending = false;
+  for (int j = 1; j <= nsteps; ++j) {
+    const long long it = h->it + 1;
+    if (int rc = one_step(h, method, pending, true)) return rc;
+    h->it = it;
+    pending = update > 0 && (it % update == 0 || it == 1 || (final_update && j == nsteps));
+  }
+  if (pending) return launch_phys(h, pal::F_UPDATE_DT);
+  return PAL_OK;
+}
+
+int pal_compute_cflm(pal_handle* h, double* cflm) {
+  if (int rc = check(h)) return rc;
+  if (int rc = launch_phys(h, 0)) return rc;
+  if (int rc = read_scalars(h)) return rc;
+  if (cflm) *cflm = h->sc_host->cflm;
+  return PAL_OK;
+}
+
+int pal_next_dt(pal_handle* h, int sync_host, double* cflm) {
+  if (int rc = check(h)) return rc;
+  if (int rc = launch_phys(h, pal::F_UPDATE_DT)) return rc;
+  if (sync_host) {
+    if (int rc = read_scalars(h)) return rc;
+    if (cflm) *cflm = h->sc_host->cflm;
+  }
+  return PAL_OK;
+}
+
+int pal_diagnostics(pal_handle* h, pal_diag* out) {
+  if (int rc = check(h)) return rc;
+  if (!out) return fail(h, PAL_ERR_INVALID, "out is null");
+  if (int rc = launch_phys(h, 0)) return rc;
+  StepArgs a = base_args(h);
+  h->ks->spectral(a, h->stream, h->spectral_blocks);
+  PAL_LAUNCHED(h, "k_spectral");
+  if (int rc = read_scalars(h)) return rc;
+  const DevScalars* s = h->sc_host;
+  out->U = std::sqrt(std::max(0.0, s->mean_speed2));
+  out->E = s->E;
+  out->Z = s->Z;
+  out->P = s->P;
+  out->kmax2 = s->kmax2;
+  out->L = s->E > 0.0 ? 2.0 * pal::kPi * s->L / s->E : NAN;
+  out->tau_l = (out->U > 0.0 && s->E > 0.0) ? out->L / out->U : NAN;
+  out->pal_over_ens_kmax2 = (s->Z > 0.0 && s->kmax2 > 0.0) ? s->P / (s->Z * s->kmax2) : 0.0;
+  out->cflm = s->cflm;
+  out->energy_joules = 0.5 * (2.0 * pal::kPi) * (2.0 * pal::kPi) * s->mean_speed2;
+  out->nonfinite = s->nonfinite;
+  if (s->nonfinite) return fail(h, PAL_ERR_NONFINITE, "NaN/Inf in the field");
+  return PAL_OK;
+}
+
+int pal_materialize_physical(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  if (!h->phys) {
+    const size_t bytes = 2 * (size_t)h->M * h->M * (h->esz / 2);
+    PAL_CK(h, cudaMalloc(&h->phys, bytes));
+  }
+  return launch_phys(h, pal::F_PHYS);
+}
+
+int pal_get_field(pal_handle* h, int which, void* host_dst) {
+  if (int rc = check(h)) return rc;
+  if (!host_dst) return fail(h, PAL_ERR_INVALID, "host_dst is null");
+  if (which == PAL_FIELD_OM2 || which == PAL_FIELD_FNM1) {
+    h->ks->transpose(which == PAL_FIELD_OM2 ? h->om : h->fnm1, h->stage, h->Nh, h->N, 1, h->stream);
+    PAL_LAUNCHED(h, "transpose out");
+    PAL_CK(h, cudaMemcpyAsync(host_dst, h->stage, (size_t)h->N * h->Nh * h->esz, cudaMemcpyDeviceToHost, h->stream));
+    PAL_CK(h, cudaStreamSynchronize(h->stream));
+    return PAL_OK;
+  }
+  if (which == PAL_FIELD_UR_U || which == PAL_FIELD_UR_V) {
+    if (int rc = pal_materialize_physical(h)) return rc;
+    const size_t plane = (size_t)h->M * h->M * (h->esz / 2);
+    const char* src = static_cast<const char*>(h->phys) + (which == PAL_FIELD_UR_V ? plane : 0);
+    PAL_CK(h, cudaMemcpyAsync(host_dst, src, plane, cudaMemcpyDeviceToHost, h->stream));
+    PAL_CK(h, cudaStreamSynchronize(h->stream));
+    return PAL_OK;
+  }
+  return fail(h, PAL_ERR_INVALID, "unknown field");
+}
+
+int pal_field_device_ptr(pal_handle* h, int which, void** ptr) {
+  if (int rc = check(h)) return rc;
+  if (!ptr) return fail(h, PAL_ERR_INVALID, "ptr is null");
+  switch (which) {
+    case PAL_FIELD_OM2: *ptr = h->om; return PAL_OK;
+    case PAL_FIELD_FNM1: *ptr = h->fnm1; return PAL_OK;
+    case PAL_FIELD_UR_U:
+    case PAL_FIELD_UR_V:
+      if (!h->phys) return fail(h, PAL_ERR_STATE, "physical planes not materialized");
+      *ptr = static_cast<char*>(h->phys) + (which == PAL_FIELD_UR_V ? (size_t)h->M * h->M * (h->esz / 2) : 0);
+      return PAL_OK;
+    default: return fail(h, PAL_ERR_INVALID, "unknown field");
+  }
+}
+
+int pal_synchronize(pal_handle* h) {
+  if (int rc = check(h)) return rc;
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+int pal_get_stream(pal_handle* h, void** stream) {
+  if (int rc = check(h)) return rc;
+  if (!stream) return fail(h, PAL_ERR_INVALID, "stream is null");
+  *stream = (void*)h->stream;
+  return PAL_OK;
+}
+
+int pal_last_error(pal_handle* h, char* buf, size_t n) {
+  if (!buf || n == 0) return PAL_ERR_INVALID;
+  const std::string& s = h ? h->err : g_err;
+  std::strncpy(buf, s.c_str(), n - 1);
+  buf[n - 1] = 0;
+  return PAL_OK;
+}
+
+}  // extern "C"

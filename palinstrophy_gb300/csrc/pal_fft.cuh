@@ -1,0 +1,288 @@
+// In-register DFT butterflies and in-place shared-memory FFT passes for the
+// 3/2-padded lines (length M = 3N/2 = 2^a 3^b) of the DNS step.
+//
+// Layout convention (all kernels): a tile of V independent lines sits in
+// shared memory as [slot][v] (v fastest), slot = k + k / RP (one pad slot per
+// RP slots, RP = radix of the last DIF pass, even, so the stride-1 middle pass
+// is bank-conflict free).  Consecutive lanes own the V lines of one butterfly,
+// so they share one twiddle load.
+//
+// Transform structure (mixed radix R0..R{NP-1}, M = prod R):
+//   DIF pass p : span L_p = M / (R0..R{p-1}), stride S_p = L_p / R_p;
+//                y = DFT_R(x[base + j S]);  y_k *= W_L^{i k};  stored in place.
+//                natural order in -> digit-reversed order out.
+//   DIT pass p : the transpose: x_k *= W_L^{i k};  y = DFT_R(x);  in place.
+//                digit-reversed in -> natural out (passes run NP-1 .. 0).
+// The last DIF pass and the first DIT pass share their butterflies, so a
+// pointwise operation between an inverse and a forward transform (the
+// products, or the spectral update) is fused into a single smem round trip.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <utility>
+
+#include "pal_consts.h"
+
+namespace pal {
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+template <typename T> using cplx = typename Cplx<T>::type;
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return {a.x + b.x, a.y + b.y}; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return {a.x - b.x, a.y - b.y}; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  return {a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y};
+}
+
+// Multiply by W_R^(SIGN*E) = cos(2 pi E/R) + i SIGN sin(2 pi E/R), all compile time.
+template <int R, int E, int SIGN, typename C>
+__device__ __forceinline__ C twc(C a) {
+  using T = decltype(a.x);
+  constexpr int e = ((E % R) + R) % R;
+  if constexpr (e == 0) {
+    return a;
+  } else if constexpr ((4 * e) % R == 0) {
+    constexpr int q = 4 * e / R;  // quarter turns
+    if constexpr (q == 2) {
+      return C{-a.x, -a.y};
+    } else if constexpr ((q == 1) == (SIGN > 0)) {
+      return C{-a.y, a.x};  // * (+i)
+    } else {
+      return C{a.y, -a.x};  // * (-i)
+    }
+  } else if constexpr ((8 * e) % R == 0) {
+    constexpr int q = 8 * e / R;  // odd multiple of pi/4
+    constexpr T h = T(0.7071067811865475244008443621);
+    constexpr T c = (q == 1 || q == 7) ? h : -h;
+    constexpr T s0 = (q == 1 || q == 3) ? h : -h;
+    constexpr T s = SIGN > 0 ? s0 : -s0;
+    return C{c * a.x - s * a.y, s * a.x + c * a.y};
+  } else {
+    constexpr T c = T(Trig<R>::c[e]);
+    constexpr T s = SIGN > 0 ? T(Trig<R>::s[e]) : T(-Trig<R>::s[e]);
+    return C{c * a.x - s * a.y, s * a.x + c * a.y};
+  }
+}
+
+template <int R, int SIGN, typename C> struct Dft;
+
+template <int SIGN, typename C> struct Dft<1, SIGN, C> {
+  static __device__ __forceinline__ void run(C*) {}
+};
+template <int SIGN, typename C> struct Dft<2, SIGN, C> {
+  static __device__ __forceinline__ void run(C* x) {
+    C a = x[0], b = x[1];
+    x[0] = cadd(a, b);
+    x[1] = csub(a, b);
+  }
+};
+template <int SIGN, typename C> struct Dft<3, SIGN, C> {
+  static __device__ __forceinline__ void run(C* x) {
+    using T = decltype(x[0].x);
+    constexpr T h = T(0.8660254037844386467637232);  // sin(2 pi / 3)
+    C t = cadd(x[1], x[2]);
+    C d = csub(x[1], x[2]);
+    C m = {x[0].x - T(0.5) * t.x, x[0].y - T(0.5) * t.y};
+    C r = SIGN > 0 ? C{-h * d.y, h * d.x} : C{h * d.y, -h * d.x};
+    x[0] = cadd(x[0], t);
+    x[1] = cadd(m, r);
+    x[2] = csub(m, r);
+  }
+};
+template <int SIGN, typename C> struct Dft<4, SIGN, C> {
+  static __device__ __forceinline__ void run(C* x) {
+    C a = cadd(x[0], x[2]), b = csub(x[0], x[2]);
+    C c = cadd(x[1], x[3]), d = csub(x[1], x[3]);
+    C e = SIGN > 0 ? C{-d.y, d.x} : C{d.y, -d.x};
+    x[0] = cadd(a, c);
+    x[2] = csub(a, c);
+    x[1] = cadd(b, e);
+    x[3] = csub(b, e);
+  }
+};
+
+template <int R, int A, int SIGN, typename C, int... I>
+__device__ __forceinline__ void inner_twiddles(C* y, std::integer_sequence<int, I...>) {
+  ((y[I] = twc<R, (I / A) * (I % A), SIGN>(y[I])), ...);
+}
+
+// R = A*B: n = B n1 + n2, k = k1 + A k2 (four-step inside registers).
+template <int A, int B, int SIGN, typename C>
+__device__ __forceinline__ void dft_ab(C* x) {
+  constexpr int R = A * B;
+  C y[R];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    C t[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) t[n1] = x[B * n1 + n2];
+    Dft<A, SIGN, C>::run(t);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = t[k1];
+  }
+  inner_twiddles<R, A, SIGN>(y, std::make_integer_sequence<int, R>{});
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) {
+    C t[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) t[n2] = y[n2 * A + k1];
+    Dft<B, SIGN, C>::run(t);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) x[k1 + A * k2] = t[k2];
+  }
+}
+
+#define PAL_COMPOSITE(R_, A_, B_)                                                         \
+  template <int SIGN, typename C> struct Dft<R_, SIGN, C> {                               \
+    static __device__ __forceinline__ void run(C* x) { dft_ab<A_, B_, SIGN, C>(x); }      \
+  };
+PAL_COMPOSITE(6, 2, 3)
+PAL_COMPOSITE(8, 2, 4)
+PAL_COMPOSITE(12, 3, 4)
+PAL_COMPOSITE(16, 4, 4)
+PAL_COMPOSITE(24, 3, 8)
+PAL_COMPOSITE(32, 4, 8)
+PAL_COMPOSITE(48, 3, 16)
+PAL_COMPOSITE(64, 8, 8)
+#undef PAL_COMPOSITE
+
+// ---------------------------------------------------------------------------
+// Plan: compile-time radix list for one line length.
+template <int M_, int... Rs>
+struct Plan {
+  static constexpr int M = M_;
+  static constexpr int NP = sizeof...(Rs);
+  static constexpr int R[NP] = {Rs...};
+  static constexpr int RP = R[NP - 1];
+  static constexpr int prod() {
+    int p = 1;
+    for (int q = 0; q < NP; ++q) p *= R[q];
+    return p;
+  }
+  static_assert(prod() == M_, "radices must multiply to M");
+  static_assert(NP >= 2, "at least two passes");
+  static_assert(RP % 2 == 0, "last radix must be even (bank-conflict-free padding)");
+  // span of pass p (the sub-transform length it works on) and its stride
+  static constexpr int span(int p) {
+    int L = M;
+    for (int q = 0; q < p; ++q) L /= R[q];
+    return L;
+  }
+  static constexpr int stride(int p) { return span(p) / R[p]; }
+  static constexpr int weight(int p) {  // frequency weight of digit p
+    int w = 1;
+    for (int q = 0; q < p; ++q) w *= R[q];
+    return w;
+  }
+  static constexpr int PADM = M + M / RP;
+  static __device__ __forceinline__ int phys(int k) { return k + k / RP; }
+  // frequency index of the DIF output stored at position pos (every constant
+  // is a template-time value, so no radix table is touched at run time)
+  template <int Q>
+  static __device__ __forceinline__ void freq_digits(int& pos, int& f) {
+    if constexpr (Q < NP) {
+      constexpr int s = stride(Q);
+      constexpr int w = weight(Q);
+      const int k = pos / s;
+      pos -= k * s;
+      f += k * w;
+      freq_digits<Q + 1>(pos, f);
+    }
+  }
+  static __device__ __forceinline__ int freq(int pos) {
+    int f = 0;
+    freq_digits<0>(pos, f);
+    return f;
+  }
+};
+
+// Twiddle W_M^(SIGN*m) from the forward table tw[m] = exp(-2 pi i m / M).
+template <int SIGN, typename C>
+__device__ __forceinline__ C twl(const C* __restrict__ tw, int m) {
+  C w = __ldg(tw + m);
+  if constexpr (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
+// One DIF pass p over a [slot][v] tile in shared memory.
+template <typename T, class PL, int V, int NT, int P, int SIGN>
+__device__ __forceinline__ void dif_pass(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  using C = cplx<T>;
+  constexpr int R = PL::R[P];
+  constexpr int L = PL::span(P);
+  constexpr int S = L / R;
+  constexpr int NB = V * (PL::M / R);
+  constexpr int TS = PL::M / L;  // twiddle table step
+  for (int w = tid; w < NB; w += NT) {
+    const int v = w % V;
+    const int b = w / V;
+    const int blk = b / S;
+    const int i = b - blk * S;
+    const int base = blk * L + i;
+    C x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = sm[PL::phys(base + j * S) * V + v];
+    Dft<R, SIGN, C>::run(x);
+    if constexpr (S > 1) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<SIGN>(tw, TS * i * k));
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) sm[PL::phys(base + k * S) * V + v] = x[k];
+  }
+}
+
+// One DIT pass p (transpose of the DIF pass).
+template <typename T, class PL, int V, int NT, int P, int SIGN>
+__device__ __forceinline__ void dit_pass(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  using C = cplx<T>;
+  constexpr int R = PL::R[P];
+  constexpr int L = PL::span(P);
+  constexpr int S = L / R;
+  constexpr int NB = V * (PL::M / R);
+  constexpr int TS = PL::M / L;
+  for (int w = tid; w < NB; w += NT) {
+    const int v = w % V;
+    const int b = w / V;
+    const int blk = b / S;
+    const int i = b - blk * S;
+    const int base = blk * L + i;
+    C x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = sm[PL::phys(base + k * S) * V + v];
+    if constexpr (S > 1) {
+#pragma unroll
+      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<SIGN>(tw, TS * i * k));
+    }
+    Dft<R, SIGN, C>::run(x);
+#pragma unroll
+    for (int j = 0; j < R; ++j) sm[PL::phys(base + j * S) * V + v] = x[j];
+  }
+}
+
+// DIF passes FROM..TO-1 (each followed by a barrier).
+template <typename T, class PL, int V, int NT, int SIGN, int P, int TO>
+__device__ __forceinline__ void dif_range(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  if constexpr (P < TO) {
+    dif_pass<T, PL, V, NT, P, SIGN>(sm, tw, tid);
+    __syncthreads();
+    dif_range<T, PL, V, NT, SIGN, P + 1, TO>(sm, tw, tid);
+  }
+}
+// DIT passes P down to TO (inclusive), each followed by a barrier.
+template <typename T, class PL, int V, int NT, int SIGN, int P, int TO>
+__device__ __forceinline__ void dit_range(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  if constexpr (P >= TO) {
+    dit_pass<T, PL, V, NT, P, SIGN>(sm, tw, tid);
+    __syncthreads();
+    dit_range<T, PL, V, NT, SIGN, P - 1, TO>(sm, tw, tid);
+  }
+}
+
+}  // namespace pal

@@ -1,0 +1,616 @@
+// Fused kernels of the GB300 DNS step.
+//
+// Device state of one field (element type T = float or double):
+//   om, fnm1 : [kx][z]  (N/2 lines of N)      spectral vorticity / last nonlinear term
+//   w0, w1   : [kx][z]  (N/2 lines of M)      the work planes, holding either
+//               U-state: velocity (u^, v^) after the inverse z-transform, or
+//               P-state: products after the forward x-transform,
+//                        A = F_x(u^2 - v^2), B = F_x(u v).
+// One stage of a step is two launches:
+//   k_row : per tile of V physical rows z: Hermitian-packed inverse x-FFT
+//           (u + i v), products, packed forward x-FFT, unpack A, B  (U -> P)
+//   k_col : per column kx: forward z-FFT of A and B, nonlinear term, CNAB2 /
+//           IMEX-RK3 update of om/fnm1, omega -> (u^, v^), de-aliasing pad,
+//           inverse z-FFT (P -> U)
+// The reference's STEP2B/STEP3/STEP2A split (turbo_simulator.py:1378-2100)
+// maps onto this as: k_row = STEP2A row half + STEP2B products + STEP2B row
+// half; k_col = STEP2B column half + STEP3 + STEP2A column half.
+#pragma once
+#include <math.h>
+
+#include "pal_fft.cuh"
+
+namespace pal {
+
+enum : int {
+  F_STATS = 1,      // k_row / k_phys: CFL max and sum(u^2+v^2) reduction
+  F_UPDATE_DT = 2,  // ... and the NEXTDT update of dt, cn from that CFLM
+  F_ADVANCE = 4,    // k_col: t += dt, it += 1 in the epilogue
+  F_CNM1 = 8,       // k_col: cnm1 = cn in the epilogue (CNAB2)
+  F_PHYS = 16,      // k_phys: store the physical u, v planes
+};
+
+// Device-resident scalars, FP64 in both precisions.
+struct DevScalars {
+  double dt, cn, cnm1, t;
+  double visc, cflnum;
+  double cflm, mean_speed2, maxabs;
+  double E, L, Z, P, kmax2;
+  long long it;
+  int nonfinite;
+  int pad_;
+  unsigned int row_counter, col_counter, diag_counter, phys_counter;
+};
+
+struct StepArgs {
+  void* w0;
+  void* w1;
+  void* om;
+  void* fnm1;
+  const void* tw;   // M forward twiddles exp(-2 pi i m / M)
+  const void* src;  // k_col_inv: velocity low band, reference layout (2, N, N/2)
+  void* phys;       // k_phys: physical planes (2, M, M)
+  DevScalars* sc;
+  double* part;     // per-block reduction partials
+  int N;
+  int flags;
+  double h1, h2;    // implicit factors: rhs = 1 - K2*h1, den = 1 + K2*h2 (if from_dt == 0)
+  double c2, c3;    // explicit weights of fn and fnm1
+  double alpha, beta;
+  int scheme;       // 0 = CNAB2 (coefficients from device dt/cnm1), 1 = RK3 stage
+};
+
+constexpr double kPi = 3.14159265358979323846;
+
+// --------------------------------------------------------------------------
+// Block reductions (deterministic: fixed tree order)
+template <int NT, int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* red /* K*NT/32 */, int tid) {
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+  }
+  constexpr int NW = NT / 32;
+  if ((tid & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) red[q * NW + (tid >> 5)] = v[q];
+  }
+  __syncthreads();
+  if (tid < 32) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      double s = tid < NW ? red[q * NW + tid] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      v[q] = s;
+    }
+  }
+  __syncthreads();
+}
+
+template <int NT>
+__device__ __forceinline__ double block_max(double m, double* red, int tid) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+  constexpr int NW = NT / 32;
+  if ((tid & 31) == 0) red[tid >> 5] = m;
+  __syncthreads();
+  if (tid < 32) {
+    double s = tid < NW ? red[tid] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, off));
+    m = s;
+  }
+  __syncthreads();
+  return m;
+}
+
+// Returns true in every thread of the block that finished last.
+__device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
+  __shared__ int is_last;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    const unsigned int ticket = atomicAdd(counter, 1u);
+    is_last = (ticket == gridDim.x * gridDim.y - 1u);
+  }
+  __syncthreads();
+  return is_last != 0;
+}
+
+// Physical-space statistics of one block: (max |u|+|v|, sum u^2+v^2) -> partials;
+// the last block reduces all partials in a fixed order and applies NEXTDT.
+template <int NT>
+__device__ void finish_stats(const StepArgs& a, double mx, double sum, int M, int tid) {
+  __shared__ double red[2 * (NT / 32)];
+  mx = block_max<NT>(mx, red, tid);
+  double s1[1] = {sum};
+  block_sum<NT, 1>(s1, red, tid);
+  if (tid == 0) {
+    a.part[2 * (blockIdx.x + gridDim.x * blockIdx.y)] = mx;
+    a.part[2 * (blockIdx.x + gridDim.x * blockIdx.y) + 1] = s1[0];
+  }
+  const bool last = last_block(&a.sc->row_counter, tid);
+  if (!last) return;
+  const int nb = gridDim.x * gridDim.y;
+  double m2 = 0.0, s2[1] = {0.0};
+  for (int q = tid; q < nb; q += NT) {
+    m2 = fmax(m2, __ldcg(a.part + 2 * q));
+    s2[0] += __ldcg(a.part + 2 * q + 1);
+  }
+  m2 = block_max<NT>(m2, red, tid);
+  block_sum<NT, 1>(s2, red, tid);
+  if (tid == 0) {
+    DevScalars* sc = a.sc;
+    const double cflm = m2 * (double(a.N) / (2.0 * kPi));
+    sc->maxabs = m2;
+    sc->cflm = cflm;
+    sc->mean_speed2 = s2[0] / (double(M) * double(M));
+    if (!isfinite(s2[0])) sc->nonfinite = 1;
+    if ((a.flags & F_UPDATE_DT) && cflm > 0.0 && sc->dt > 0.0) {
+      const double cfl = cflm * sc->dt * kPi;
+      const double cn = 0.8 + 0.2 * (sc->cflnum / cfl);
+      sc->cn = cn;
+      sc->dt = sc->dt * cn;
+    }
+    sc->row_counter = 0u;
+  }
+}
+
+// --------------------------------------------------------------------------
+// First DIF pass of the inverse x-transform, reading the U planes directly:
+// Z[k] = u^[k] + i v^[k] (k < N/2; real parts only at k = 0),
+// Z[M-k] = conj(u^[k]) + i conj(v^[k]), zero elsewhere (the 3/2 pad).
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, int z0, int tid) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  const C* __restrict__ w0 = static_cast<const C*>(a.w0);
+  const C* __restrict__ w1 = static_cast<const C*>(a.w1);
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  const int Nh = a.N >> 1;
+  for (int w = tid; w < V * S; w += NT) {
+    const int v = w % V;
+    const int i = w / V;
+    const int z = z0 + v;
+    C x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int k = i + j * S;
+      C zz = {T(0), T(0)};
+      if (k < Nh) {
+        const C u = w0[(size_t)k * M + z];
+        const C q = w1[(size_t)k * M + z];
+        zz = (k == 0) ? C{u.x, q.x} : C{u.x - q.y, u.y + q.x};
+      } else if (k > M - Nh) {
+        const int m = M - k;
+        const C u = w0[(size_t)m * M + z];
+        const C q = w1[(size_t)m * M + z];
+        zz = C{u.x + q.y, q.x - u.y};
+      }
+      x[j] = zz;
+    }
+    Dft<R, +1, C>::run(x);
+#pragma unroll
+    for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<+1>(tw, i * k));
+#pragma unroll
+    for (int k = 0; k < R; ++k) sm[PL::phys(i + k * S) * V + v] = x[k];
+  }
+  __syncthreads();
+}
+
+// k_row: U-state rows -> P-state rows (products), optional CFL statistics.
+template <typename T, class PL, int V, int NT>
+__global__ void __launch_bounds__(NT) k_row(StepArgs a) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int M = PL::M;
+  const int tid = threadIdx.x;
+  const int z0 = blockIdx.x * V;
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+
+  row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
+  dif_range<T, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
+
+  // middle: last inverse DIF pass -> products -> first forward DIT pass
+  const bool stats = (a.flags & F_STATS) != 0;
+  T mx = T(0), acc = T(0), comp = T(0);
+  {
+    constexpr int R = PL::RP;
+    constexpr int NB = V * (M / R);
+    for (int w = tid; w < NB; w += NT) {
+      const int v = w % V;
+      const int b = w / V;
+      C x[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) x[j] = sm[PL::phys(b * R + j) * V + v];
+      Dft<R, +1, C>::run(x);
+      if (stats) {
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+          const T u = x[j].x, q = x[j].y;
+          mx = fmax(mx, fabs(u) + fabs(q));
+          const T y = (u * u + q * q) - comp;  // Kahan
+          const T t = acc + y;
+          comp = (t - acc) - y;
+          acc = t;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const T u = x[j].x, q = x[j].y;
+        x[j] = C{u * u - q * q, u * q};
+      }
+      Dft<R, -1, C>::run(x);
+#pragma unroll
+      for (int j = 0; j < R; ++j) sm[PL::phys(b * R + j) * V + v] = x[j];
+    }
+    __syncthreads();
+  }
+  dit_range<T, PL, V, NT, -1, PL::NP - 2, 0>(sm, tw, tid);
+
+  // unpack P = FFT(a + i b) into A = F(a), B = F(b) for kx < N/2 and store
+  {
+    C* __restrict__ w0 = static_cast<C*>(a.w0);
+    C* __restrict__ w1 = static_cast<C*>(a.w1);
+    const int Nh = a.N >> 1;
+    for (int w = tid; w < V * Nh; w += NT) {
+      const int v = w % V;
+      const int k = w / V;
+      const C p = sm[PL::phys(k) * V + v];
+      const C q = sm[PL::phys(k == 0 ? 0 : M - k) * V + v];
+      w0[(size_t)k * M + z0 + v] = C{T(0.5) * (p.x + q.x), T(0.5) * (p.y - q.y)};
+      w1[(size_t)k * M + z0 + v] = C{T(0.5) * (p.y + q.y), T(-0.5) * (p.x - q.x)};
+    }
+  }
+  if (stats) finish_stats<NT>(a, double(mx), double(acc) - double(comp), M, tid);
+}
+
+// k_phys: U-state rows -> physical u, v (statistics, optional plane store).
+template <typename T, class PL, int V, int NT>
+__global__ void __launch_bounds__(NT) k_phys(StepArgs a) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int M = PL::M;
+  const int tid = threadIdx.x;
+  const int z0 = blockIdx.x * V;
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
+  dif_range<T, PL, V, NT, +1, 1, PL::NP>(sm, tw, tid);
+  T mx = T(0), acc = T(0), comp = T(0);
+  T* __restrict__ ph = static_cast<T*>(a.phys);
+  const bool store = (a.flags & F_PHYS) != 0;
+  for (int w = tid; w < V * M; w += NT) {
+    const int v = w % V;
+    const int pos = w / V;
+    const C val = sm[PL::phys(pos) * V + v];
+    mx = fmax(mx, fabs(val.x) + fabs(val.y));
+    const T y = (val.x * val.x + val.y * val.y) - comp;
+    const T t = acc + y;
+    comp = (t - acc) - y;
+    acc = t;
+    if (store) {
+      const int n = PL::freq(pos);
+      ph[(size_t)(z0 + v) * M + n] = val.x;
+      ph[(size_t)M * M + (size_t)(z0 + v) * M + n] = val.y;
+    }
+  }
+  finish_stats<NT>(a, double(mx), double(acc) - double(comp), M, tid);
+}
+
+// --------------------------------------------------------------------------
+// Spectral update of one mode (kx, z) and the omega -> velocity inversion.
+// CNAB2 (turbo_simulator.py:1642-1652) and LS-IMEX-RK3 (1826-1837) share the
+// form  om' = [(1 - K2 h1) om + c2 fn + c3 fnm1] / (1 + K2 h2).
+template <typename T>
+struct ModeCoef {
+  T h1, h2, c2, c3, divxz;
+};
+
+// k_col: P-state column -> (om, fnm1 update) -> U-state column.
+template <typename T, class PL, int NT>
+__global__ void __launch_bounds__(NT) k_col(StepArgs a) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int M = PL::M;
+  constexpr int V = 2;
+  const int tid = threadIdx.x;
+  const int kx = blockIdx.x;
+  const int N = a.N, Nh = N >> 1;
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  C* __restrict__ w0 = static_cast<C*>(a.w0);
+  C* __restrict__ w1 = static_cast<C*>(a.w1);
+  C* __restrict__ om = static_cast<C*>(a.om) + (size_t)kx * N;
+  C* __restrict__ fm = static_cast<C*>(a.fnm1) + (size_t)kx * N;
+
+  // implicit / explicit weights, formed in FP64 from the device scalars
+  ModeCoef<T> cf;
+  {
+    const DevScalars* sc = a.sc;
+    const double dt = sc->dt, visc = sc->visc;
+    double h1, h2, c2, c3;
+    if (a.scheme == 0) {
+      const double cnm1 = sc->cnm1;
+      h1 = h2 = (0.5 * visc) * dt;
+      c2 = (0.5 * dt) * (2.0 + cnm1);
+      c3 = (-0.5 * dt) * cnm1;
+    } else {
+      h1 = (a.beta * dt) * visc;
+      h2 = (a.alpha * dt) * visc;
+      c2 = a.alpha * dt;
+      c3 = a.beta * dt;
+    }
+    cf.h1 = T(h1);
+    cf.h2 = T(h2);
+    cf.c2 = T(c2);
+    cf.c3 = T(c3);
+    const T m32 = T(1.5) * T(N);
+    cf.divxz = T(1) / (m32 * m32);
+  }
+
+  // pass 0 (forward z-DIF) straight from the P planes
+  {
+    constexpr int R = PL::R[0];
+    constexpr int S = M / R;
+    for (int w = tid; w < V * S; w += NT) {
+      const int v = w & 1;
+      const int i = w >> 1;
+      const C* __restrict__ src = (v == 0 ? w0 : w1) + (size_t)kx * M;
+      C x[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) x[j] = src[i + j * S];
+      Dft<R, -1, C>::run(x);
+#pragma unroll
+      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<-1>(tw, i * k));
+#pragma unroll
+      for (int k = 0; k < R; ++k) sm[PL::phys(i + k * S) * V + v] = x[k];
+    }
+    __syncthreads();
+  }
+  dif_range<T, PL, V, NT, -1, 1, PL::NP - 1>(sm, tw, tid);
+
+  // middle: last forward DIF -> nonlinear term, update, inversion -> first inverse DIT
+  {
+    constexpr int R = PL::RP;
+    constexpr int NB = V * (M / R);
+    constexpr int FSTEP = M / R;
+    const T ax = T(kx);
+    for (int w0i = 0; w0i < NB; w0i += NT) {
+      const int w = w0i + tid;
+      const bool act = w < NB;
+      const int v = w & 1;
+      const int b = act ? (w >> 1) : 0;
+      C x[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) x[j] = act ? sm[PL::phys(b * R + j) * V + v] : C{T(0), T(0)};
+      Dft<R, -1, C>::run(x);
+      const int fb = PL::freq(b * R);
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const int f = fb + j * FSTEP;
+        const bool inband = act && (f < Nh || f >= N);
+        const int z = f < Nh ? f : f - Nh;
+        const C mine = x[j];
+        C oth;
+        oth.x = __shfl_xor_sync(0xffffffffu, mine.x, 1);
+        oth.y = __shfl_xor_sync(0xffffffffu, mine.y, 1);
+        C ld = {T(0), T(0)};
+        if (inband) ld = (v == 0) ? om[z] : fm[z];
+        C ldo;
+        ldo.x = __shfl_xor_sync(0xffffffffu, ld.x, 1);
+        ldo.y = __shfl_xor_sync(0xffffffffu, ld.y, 1);
+        C res = {T(0), T(0)};
+        if (inband) {
+          const C Az = v == 0 ? mine : oth;
+          const C Bz = v == 0 ? oth : mine;
+          const C o = v == 0 ? ld : ldo;
+          const C fo = v == 0 ? ldo : ld;
+          const T gz = T(z < Nh ? z : z - N);
+          const T K2 = ax * ax + gz * gz;
+          const T GA = gz * ax;
+          const T G2mA2 = gz * gz - ax * ax;
+          C fn = {T(0), T(0)};
+          if (z != Nh) {
+            fn.x = (Az.x * GA + Bz.x * G2mA2) * cf.divxz;
+            fn.y = (Az.y * GA + Bz.y * G2mA2) * cf.divxz;
+          }
+          const T c1 = T(1) - K2 * cf.h1;
+          const T rden = T(1) / (T(1) + K2 * cf.h2);
+          C on;
+          on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
+          on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
+          if (v == 0) {
+            om[z] = on;
+          } else {
+            fm[z] = fn;
+          }
+          if (kx >= 1) {
+            const T ik = T(1) / K2;
+            const C t = {on.x * ik, on.y * ik};
+            res = (v == 0) ? C{t.y * gz, -t.x * gz} : C{-t.y * ax, t.x * ax};
+          } else if (v == 0 && z >= 1) {
+            const T ig = T(1) / gz;
+            res = C{on.y * ig, -on.x * ig};
+          }
+        }
+        x[j] = res;
+      }
+      Dft<R, +1, C>::run(x);
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < R; ++j) sm[PL::phys(b * R + j) * V + v] = x[j];
+      }
+    }
+    __syncthreads();
+  }
+  dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
+
+  // last inverse DIT pass straight into the U planes
+  {
+    constexpr int R = PL::R[0];
+    constexpr int S = M / R;
+    for (int w = tid; w < V * S; w += NT) {
+      const int v = w & 1;
+      const int i = w >> 1;
+      C* __restrict__ dst = (v == 0 ? w0 : w1) + (size_t)kx * M;
+      C x[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) x[k] = sm[PL::phys(i + k * S) * V + v];
+#pragma unroll
+      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<+1>(tw, i * k));
+      Dft<R, +1, C>::run(x);
+#pragma unroll
+      for (int j = 0; j < R; ++j) dst[i + j * S] = x[j];
+    }
+  }
+  if (a.flags & (F_ADVANCE | F_CNM1)) {
+    if (last_block(&a.sc->col_counter, tid) && tid == 0) {
+      DevScalars* sc = a.sc;
+      if (a.flags & F_ADVANCE) {
+        sc->t += sc->dt;
+        sc->it += 1;
+      }
+      if (a.flags & F_CNM1) sc->cnm1 = sc->cn;
+      sc->col_counter = 0u;
+    }
+  }
+}
+
+// k_col_inv: velocity low band -> pad -> inverse z-FFT -> U planes.  The low
+// band comes from `src` (reference layout (2, N, N/2), e.g. the generator's
+// uc_full) or, when src is null, from the omega -> velocity inversion of om
+// (turbo_simulator.py:1555-1585).
+template <typename T, class PL, int NT>
+__global__ void __launch_bounds__(NT) k_col_inv(StepArgs a) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int M = PL::M;
+  constexpr int V = 2;
+  const int tid = threadIdx.x;
+  const int kx = blockIdx.x;
+  const int N = a.N, Nh = N >> 1;
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  const C* __restrict__ src = static_cast<const C*>(a.src);
+  const C* __restrict__ om = static_cast<const C*>(a.om) + (size_t)kx * N;
+  for (int w = tid; w < V * M; w += NT) {
+    const int v = w & 1;
+    const int pos = w >> 1;
+    const int f = PL::freq(pos);
+    C val = {T(0), T(0)};
+    if (f < Nh || f >= N) {
+      const int z = f < Nh ? f : f - Nh;
+      if (src != nullptr) {
+        val = src[(size_t)v * N * Nh + (size_t)z * Nh + kx];
+      } else {
+        const C o = om[z];
+        const T gz = T(z < Nh ? z : z - N);
+        const T ax = T(kx);
+        if (kx >= 1) {
+          const T ik = T(1) / (ax * ax + gz * gz);
+          const C t = {o.x * ik, o.y * ik};
+          val = (v == 0) ? C{t.y * gz, -t.x * gz} : C{-t.y * ax, t.x * ax};
+        } else if (v == 0 && z >= 1) {
+          const T ig = T(1) / gz;
+          val = C{o.y * ig, -o.x * ig};
+        }
+      }
+    }
+    sm[PL::phys(pos) * V + v] = val;
+  }
+  __syncthreads();
+  dit_range<T, PL, V, NT, +1, PL::NP - 1, 0>(sm, tw, tid);
+  C* __restrict__ w0 = static_cast<C*>(a.w0);
+  C* __restrict__ w1 = static_cast<C*>(a.w1);
+  for (int w = tid; w < V * M; w += NT) {
+    const int v = w & 1;
+    const int k = w >> 1;
+    (v == 0 ? w0 : w1)[(size_t)kx * M + k] = sm[PL::phys(k) * V + v];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Spectral sums over om [kx][z]: E = sum w |om|^2/K2, Lsum = sum w |om|^2/K2^1.5,
+// Z = sum w |om|^2 (minus the (0,0) mode), P = sum w K2 |om|^2, with the
+// rfft weights w = [1, 2, ..., 2, 1] of turbo_simulator.py:778-781 and
+// turbo_main.py:2040-2044.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_spectral(StepArgs a) {
+  using C = cplx<T>;
+  const C* __restrict__ om = static_cast<const C*>(a.om);
+  const int N = a.N, Nh = N >> 1;
+  const long long total = (long long)N * Nh;
+  const int tid = threadIdx.x;
+  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  int bad = 0;
+  for (long long idx = (long long)blockIdx.x * NT + tid; idx < total; idx += (long long)gridDim.x * NT) {
+    const int kx = int(idx / N);
+    const int z = int(idx - (long long)kx * N);
+    const C o = om[idx];
+    const double p = double(o.x) * double(o.x) + double(o.y) * double(o.y);
+    if (!isfinite(p)) bad = 1;
+    const double gz = double(z < Nh ? z : z - N);
+    const double K2 = double(kx) * double(kx) + gz * gz;
+    const double wt = (kx == 0 || kx == Nh - 1) ? 1.0 : 2.0;
+    if (K2 > 0.0) {
+      const double e = wt * p / K2;
+      s[0] += e;
+      s[1] += e / sqrt(K2);
+    } else {
+      s[4] += p;  // the (0,0) mode, removed from Z
+    }
+    s[2] += wt * p;
+    s[3] += wt * K2 * p;
+  }
+  __shared__ double red[5 * (NT / 32)];
+  block_sum<NT, 5>(s, red, tid);
+  if (bad) atomicOr(&a.sc->nonfinite, 1);
+  if (tid == 0) {
+#pragma unroll
+    for (int q = 0; q < 5; ++q) a.part[5 * blockIdx.x + q] = s[q];
+  }
+  if (!last_block(&a.sc->diag_counter, tid)) return;
+  double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int q = tid; q < (int)gridDim.x; q += NT) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) t[r] += __ldcg(a.part + 5 * q + r);
+  }
+  block_sum<NT, 5>(t, red, tid);
+  if (tid == 0) {
+    DevScalars* sc = a.sc;
+    sc->E = t[0];
+    sc->L = t[1];
+    sc->Z = t[2] - t[4];
+    sc->P = t[3];
+    sc->kmax2 = double(Nh - 1) * double(Nh - 1) + double(Nh) * double(Nh);
+    sc->diag_counter = 0u;
+  }
+}
+
+// Layout transposes between the reference's (rows, cols) and the device's
+// (cols, rows) for complex planes; batch = gridDim.z planes.
+template <typename T>
+__global__ void k_transpose(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int rows, int cols) {
+  __shared__ cplx<T> tile[32][33];
+  const size_t plane = (size_t)rows * cols;
+  in += plane * blockIdx.z;
+  out += plane * blockIdx.z;
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    const int r = r0 + dy, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) tile[dy][threadIdx.x] = in[(size_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    const int c = c0 + dy, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) out[(size_t)c * rows + r] = tile[threadIdx.x][dy];
+  }
+}
+
+}  // namespace pal

@@ -1,0 +1,416 @@
+"""Drop-in GB300 backend for palinstrophy's DNS stepping/initialisation API.
+
+The names, signatures and DnsState fields mirror
+``palinstrophy/turbo_simulator.py`` so that its callers (``run_dns``, the
+``turbo_wrapper.DnsSimulator`` facade and the GUI) run unchanged with
+``backend="gb300"``:
+
+  create_dns_state      turbo_simulator.py:878-1054
+  dns_step2a            turbo_simulator.py:1949-2100
+  dns_step2b            turbo_simulator.py:1378-1513
+  dns_step3             turbo_simulator.py:1588-1771
+  dns_step_ls_imex_rk3  turbo_simulator.py:1900-1943
+  compute_cflm          turbo_simulator.py:2106-2125
+  next_dt               turbo_simulator.py:2127-2167
+  sync_time_scalars_from_device  turbo_simulator.py:846-854
+  DnsState.flow_eddy_metrics     turbo_simulator.py:764-810
+  run_dns / compare_time_steppers turbo_simulator.py:2744-2903
+
+Every step runs in the hand-written sm_103a kernels of libpalgpu.so; there is
+no CPU path here.  Array fields (om2, fnm1, ur_full, ...) are host NumPy copies
+taken on access, as the reference GUI does with cp.asnumpy at frame pulls.
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+import time
+from typing import Literal
+
+import numpy as np
+
+from . import _lib as L
+
+SCIPYTURBO_SEED_ENV = "SCIPYTURBO_SEED"
+PAO_SEED_MIN = 1
+PAO_SEED_MAX = 5010
+TimeStepper = Literal["CNAB2", "LS_IMEX_RK3", "CHECK"]
+SPECTRUM = Literal["PAO", "KM3"]
+_METHODS = {"CNAB2": L.PAL_CNAB2, "LS_IMEX_RK3": L.PAL_LS_IMEX_RK3}
+_PREC = {"fp32": L.PAL_FP32, "fp64": L.PAL_FP64}
+
+
+def pao_seed_from_env(default: int | None = None) -> int | None:
+    """Seed from $SCIPYTURBO_SEED, validated to 1..5010 (turbo_simulator.py:54-73)."""
+    raw = os.environ.get(SCIPYTURBO_SEED_ENV)
+    if raw is None or raw.strip() == "":
+        return default
+    try:
+        seed = int(raw.strip(), 10)
+    except ValueError as exc:
+        raise ValueError(f"{SCIPYTURBO_SEED_ENV} must be an integer from {PAO_SEED_MIN} to "
+                         f"{PAO_SEED_MAX}; got {raw!r}") from exc
+    if not PAO_SEED_MIN <= seed <= PAO_SEED_MAX:
+        raise ValueError(f"{SCIPYTURBO_SEED_ENV} must be from {PAO_SEED_MIN} to {PAO_SEED_MAX}; got {seed}")
+    return seed
+
+
+class Field:
+    """One N x N field on the GPU: owns a pal_handle and its device state."""
+
+    def __init__(self, N: int, precision: str = "fp32", Re: float = 1e4, cfl: float = 0.75):
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.lib = L.load()
+        self.N = int(N)
+        self.M = 3 * self.N // 2
+        self.precision = precision
+        self.cdt = np.complex64 if precision == "fp32" else np.complex128
+        self.rdt = np.float32 if precision == "fp32" else np.float64
+        h = L._H()
+        L.check(self.lib.pal_create(self.N, _PREC[precision], float(Re), float(cfl), h))
+        self.h = h
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pal_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        return L.check(rc, self.h)
+
+    # -- state ------------------------------------------------------------
+    def set_state(self, om2, fnm1=None, uc_low=None):
+        om2 = np.ascontiguousarray(om2, dtype=self.cdt)
+        if om2.shape != (self.N, self.N // 2):
+            raise ValueError(f"om2 must have shape {(self.N, self.N // 2)}")
+        f = None if fnm1 is None else np.ascontiguousarray(fnm1, dtype=self.cdt)
+        self._ck(self.lib.pal_set_spectral_state(self.h, L.ptr(om2), None if f is None else L.ptr(f)))
+        if uc_low is not None:
+            uc = np.ascontiguousarray(uc_low, dtype=self.cdt)
+            if uc.shape != (2, self.N, self.N // 2):
+                raise ValueError(f"uc_low must have shape {(2, self.N, self.N // 2)}")
+            self._ck(self.lib.pal_set_velocity_spectrum(self.h, L.ptr(uc)))
+
+    def set_scalars(self, t=0.0, dt=0.0, cn=1.0, cnm1=0.0, visc=1e-4, cflnum=0.75, it=0):
+        self._ck(self.lib.pal_set_scalars(self.h, t, dt, cn, cnm1, visc, cflnum, int(it)))
+
+    def set_scalar(self, which: str, value):
+        idx = {"t": L.PAL_SC_T, "dt": L.PAL_SC_DT, "cn": L.PAL_SC_CN, "cnm1": L.PAL_SC_CNM1,
+               "visc": L.PAL_SC_VISC, "cflnum": L.PAL_SC_CFLNUM, "it": L.PAL_SC_IT}[which]
+        self._ck(self.lib.pal_set_scalar(self.h, idx, float(value)))
+
+    def scalars(self) -> dict:
+        v = [L._D() for _ in range(6)]
+        it = L.ctypes.c_longlong()
+        self._ck(self.lib.pal_get_scalars(self.h, *[L.ctypes.byref(x) for x in v], L.ctypes.byref(it)))
+        return dict(zip(("t", "dt", "cn", "cnm1", "visc", "cflnum"), [x.value for x in v]), it=it.value)
+
+    # -- stepping -----------------------------------------------------------
+    def step2a(self):
+        self._ck(self.lib.pal_step2a(self.h))
+
+    def step2b(self):
+        self._ck(self.lib.pal_step2b(self.h))
+
+    def step3(self):
+        self._ck(self.lib.pal_step3(self.h))
+
+    def step_rk3(self):
+        self._ck(self.lib.pal_step_rk3(self.h))
+
+    def step(self, method="CNAB2", nsteps=1, update=0, final_update=False):
+        self._ck(self.lib.pal_step(self.h, _METHODS[method], int(nsteps), int(update), int(bool(final_update))))
+
+    def compute_cflm(self) -> float:
+        c = L._D()
+        self._ck(self.lib.pal_compute_cflm(self.h, L.ctypes.byref(c)))
+        return c.value
+
+    def next_dt(self, sync_host=True):
+        c = L._D()
+        self._ck(self.lib.pal_next_dt(self.h, int(bool(sync_host)), L.ctypes.byref(c)))
+        return c.value if sync_host else None
+
+    def diagnostics(self) -> dict:
+        d = L.PalDiag()
+        rc = self.lib.pal_diagnostics(self.h, L.ctypes.byref(d))
+        out = {n: getattr(d, n) for n, _ in L.PalDiag._fields_}
+        if rc == L.PAL_ERR_NONFINITE:
+            return out
+        self._ck(rc)
+        return out
+
+    def synchronize(self):
+        self._ck(self.lib.pal_synchronize(self.h))
+
+    def stream_ptr(self) -> int:
+        p = L._P()
+        self._ck(self.lib.pal_get_stream(self.h, L.ctypes.byref(p)))
+        return p.value
+
+    # -- fields -------------------------------------------------------------
+    def om2(self):
+        a = np.empty((self.N, self.N // 2), self.cdt)
+        self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_OM2, L.ptr(a)))
+        return a
+
+    def fnm1(self):
+        a = np.empty((self.N, self.N // 2), self.cdt)
+        self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_FNM1, L.ptr(a)))
+        return a
+
+    def ur(self, comp: int):
+        a = np.empty((self.M, self.M), self.rdt)
+        self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_UR_U if comp == 0 else L.PAL_FIELD_UR_V, L.ptr(a)))
+        return a
+
+    def device_ptr(self, which: int) -> int:
+        p = L._P()
+        self._ck(self.lib.pal_field_device_ptr(self.h, which, L.ctypes.byref(p)))
+        return p.value
+
+
+class DnsState:
+    """GB300 twin of the reference DnsState (turbo_simulator.py:654-810).
+
+    Scalars dt/cn/cnm1 are host mirrors of device values: assigning them writes
+    through to the device (turbo_simulator.py:742-753) and
+    sync_time_scalars_from_device refreshes them; visc and cflnum (changed at
+    run time by the GUI) write through as well.
+    """
+
+    _MIRRORED = {"dt", "cn", "cnm1", "visc", "cflnum"}
+
+    def __init__(self, N, Re, K0, CFL, seed, start_spectrum, precision, populate_compact_ur):
+        object.__setattr__(self, "_field", None)
+        self.backend = "gb300"
+        self.xp = np
+        self.precision = precision
+        self.Nbase = self.NX = self.NZ = int(N)
+        self.NX_full = self.NZ_full = 3 * self.NX // 2
+        self.NK_full = self.NX_full // 2 + 1
+        self.NK = 3 * self.NX // 4 + 1
+        self.Re = Re
+        self.K0 = K0
+        self.start_spectrum = start_spectrum
+        self.seed_init = int(seed)
+        self.populate_compact_ur = populate_compact_ur
+        self.fft_workers = 1
+        self.inv_dx = float(N) / (2.0 * math.pi)
+        self.t = 0.0
+        self.it = 0
+        nh = self.NX // 2
+        self.alfa = np.arange(nh, dtype=np.float32)
+        kz = np.arange(self.NZ)
+        self.gamma = np.where(kz < nh, kz, kz - self.NZ).astype(np.float32)
+        self.step3_K2 = (self.alfa[None, :] ** 2 + self.gamma[:, None] ** 2).astype(np.float32)
+        f = Field(N, precision, Re, CFL)
+        object.__setattr__(self, "_field", f)
+        object.__setattr__(self, "visc", float(np.float32(1.0 / float(np.float32(Re)))))
+        object.__setattr__(self, "cflnum", float(CFL))
+        object.__setattr__(self, "dt", 0.0)
+        object.__setattr__(self, "cn", 1.0)
+        object.__setattr__(self, "cnm1", 0.0)
+
+    def __setattr__(self, name, value):
+        object.__setattr__(self, name, value)
+        f = self.__dict__.get("_field")
+        if f is not None and name in self._MIRRORED:
+            f.set_scalar(name, float(value))
+
+    @property
+    def field(self) -> Field:
+        return self._field
+
+    def sync(self):
+        self._field.synchronize()
+
+    # -- array views (host copies) -----------------------------------------
+    @property
+    def om2(self):
+        return self._field.om2()
+
+    @property
+    def fnm1(self):
+        return self._field.fnm1()
+
+    @property
+    def ur_full(self):
+        u = self._field.ur(0)
+        out = np.zeros((3, self.NZ_full, self.NX_full), u.dtype)
+        out[0] = u
+        out[1] = self._field.ur(1)
+        return out
+
+    @property
+    def ur(self):
+        n, m = self.NX, self.NX_full
+        off = (m - n) // 2
+        full = self.ur_full
+        out = np.zeros((n, n, 3), full.dtype)
+        out[:, :, 0] = full[0, off:off + n, off:off + n]
+        out[:, :, 1] = full[1, off:off + n, off:off + n]
+        return out
+
+    def set_spectral_state(self, om2, fnm1=None, uc_low=None):
+        """Load om2/fnm1 (and optionally the velocity low band) from host arrays."""
+        self._field.set_state(om2, fnm1, uc_low)
+
+    def flow_eddy_metrics(self):
+        """(U, L, tau_L) as turbo_simulator.py:764-810 computes them."""
+        d = self._field.diagnostics()
+        return d["U"], d["L"], d["tau_l"]
+
+    def diagnostics(self) -> dict:
+        return self._field.diagnostics()
+
+
+def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float = 0.75,
+                     backend: str = "gb300", seed: int = 1, skip_pao: bool = False,
+                     populate_compact_ur: bool = True, start_spectrum: SPECTRUM = "KM3",
+                     precision: str = "fp32") -> DnsState:
+    """Allocate the GB300 state and run the PAO/KM3 generator (turbo_simulator.py:878-1054)."""
+    if backend not in ("gb300", "gpu", "auto"):
+        raise ValueError(f"backend {backend!r}: this module is the GB300 backend (no CPU path)")
+    S = DnsState(N, Re, K0, CFL, seed, start_spectrum, precision, populate_compact_ur)
+    if skip_pao:
+        return S
+    om2, uc, st = L.pao_generate(N, K0, Re, seed, start_spectrum)
+    print(f"--- INITIALIZING GB300 --- N={N}, K0={int(K0)}, Re={float(Re):,.1f}, {start_spectrum}")
+    print(f" Energy      = {st['Energy']:.8g}")
+    print(f" WiWi        = {st['WiWi']:.8g}")
+    print(f" Viscosity   = {st['visc']:.8g}")
+    print(f" PAO seed in = {seed}")
+    print(f" PAO seed out= {st['seed_out']}")
+    S.set_spectral_state(om2, None, uc)
+    S.visc = float(st["visc"])
+    S.dt, S.cn, S.cnm1 = 0.0, 1.0, 0.0
+    return S
+
+
+def dns_step2a(S: DnsState) -> None:
+    S.field.step2a()
+
+
+def dns_step2b(S: DnsState) -> None:
+    S.field.step2b()
+
+
+def dns_step3(S: DnsState, fuse: bool = True) -> None:
+    S.field.step3()
+    object.__setattr__(S, "cnm1", float(S.cn))
+
+
+def dns_step_ls_imex_rk3(S: DnsState) -> None:
+    S.field.step_rk3()
+
+
+def compute_cflm(S: DnsState) -> float:
+    return S.field.compute_cflm()
+
+
+def sync_time_scalars_from_device(S: DnsState) -> None:
+    sc = S.field.scalars()
+    for k in ("dt", "cn", "cnm1"):
+        object.__setattr__(S, k, sc[k])
+
+
+def next_dt(S: DnsState, sync_host: bool = False):
+    """NEXTDT on the device; with sync_host the host mirrors are refreshed and CFLM returned."""
+    cflm = S.field.next_dt(sync_host)
+    if sync_host:
+        sync_time_scalars_from_device(S)
+        return cflm
+    return None
+
+
+def _init_dt(S: DnsState) -> float:
+    dns_step2a(S)
+    cflm0 = compute_cflm(S)
+    S.dt = S.cflnum / (cflm0 * math.pi)
+    S.cn = 1.0
+    S.cnm1 = 0.0
+    S.t = 0.0
+    return cflm0
+
+
+def run_dns(N: int = 8, Re: float = 100, K0: float = 10.0, STEPS: int = 2, CFL: float = 0.75,
+            backend: str = "gb300", start_spectrum: SPECTRUM = "KM3", UPDATE: int = 100,
+            method: TimeStepper = "CNAB2", precision: str = "fp32"):
+    """The sim CLI driver (turbo_simulator.py:2744-2858) on the GB300 kernels."""
+    if method == "CHECK":
+        compare_time_steppers(N, Re, K0, STEPS, CFL, backend, start_spectrum, UPDATE, precision)
+        return None
+    if method not in _METHODS:
+        raise ValueError(f"unknown time stepper: {method}")
+    print("--- RUN DNS (GB300) ---")
+    print(f" N = {N}  Re = {Re}  K0 = {K0}  Steps = {STEPS}  CFL = {CFL}  Update = {UPDATE}  "
+          f"Spectrum = {start_spectrum}  Method = {method}  precision = {precision}")
+    seed = pao_seed_from_env(1)
+    S = create_dns_state(N=N, Re=Re, K0=K0, CFL=CFL, backend=backend, seed=seed,
+                         start_spectrum=start_spectrum, populate_compact_ur=False, precision=precision)
+    cflm0 = _init_dt(S)
+    print(f" [NEXTDT INIT] CFLM={cflm0:11.4f} DT={S.dt:11.7f} CN={S.cn:11.7f}")
+    f = S.field
+    f.set_scalar("it", 0)
+    f.set_scalar("t", 0.0)
+    S.sync()
+    t0 = time.perf_counter()
+    marks = sorted({1, STEPS} | set(range(UPDATE, STEPS + 1, UPDATE))) if UPDATE > 0 else [STEPS]
+    done = 0
+    for m in marks:
+        f.step(method, m - done, update=0, final_update=False)
+        done = m
+        before = f.scalars()  # t already includes this step's dt_old
+        cflm = next_dt(S, sync_host=True)
+        S.t, S.it = before["t"], before["it"]
+        _, _, tau_l = S.flow_eddy_metrics()
+        print(f" ITERATION {m:6d} T={before['t'] - before['dt']:12.10f} DT={S.dt:10.8f} "
+              f"CN={S.cn:10.8f} CFLM={cflm:.6f} TAU_L={tau_l:.6f}")
+    S.sync()
+    elap = time.perf_counter() - t0
+    fps = STEPS / elap if elap > 0 else 0.0
+    print(f" Elapsed time for {STEPS} steps (s) = {elap:.8g}")
+    print(f" Final T={S.t:.8g}  CN={S.cn:.8g}  DT={S.dt:.8g}")
+    print(f" FPS = {fps:.8g}")
+    return S
+
+
+def compare_time_steppers(N, Re, K0, STEPS, CFL, backend, start_spectrum, UPDATE, precision="fp32"):
+    """CHECK mode: CNAB2 vs LS-IMEX-RK3 from the same seed (turbo_simulator.py:2877-2903)."""
+    a = run_dns(N, Re, K0, STEPS, CFL, backend, start_spectrum, UPDATE, "CNAB2", precision)
+    b = run_dns(N, Re, K0, STEPS, CFL, backend, start_spectrum, UPDATE, "LS_IMEX_RK3", precision)
+    oa, ob = a.om2.astype(np.complex128), b.om2.astype(np.complex128)
+    l2 = float(np.linalg.norm(ob - oa) / max(np.linalg.norm(oa), 1e-30))
+    linf = float(np.abs(ob - oa).max() / max(np.abs(oa).max(), 1e-30))
+    print("--- CHECK RESULT ---")
+    print(f" OM2 relative L2={l2:.6e} Linf={linf:.6e}")
+    return l2, linf
+
+
+def main():
+    args = sys.argv[1:]
+    N = int(args[0]) if len(args) > 0 else 512
+    Re = float(args[1]) if len(args) > 1 else 10000
+    K0 = float(args[2]) if len(args) > 2 else 10.0
+    STEPS = int(args[3]) if len(args) > 3 else 1001
+    CFL = float(args[4]) if len(args) > 4 else 0.25
+    UPDATE = int(float(args[6])) if len(args) > 6 else 100
+    SPEC = args[7].upper() if len(args) > 7 else "KM3"
+    METHOD = args[8].upper() if len(args) > 8 else "CNAB2"
+    PREC = args[9].lower() if len(args) > 9 else "fp32"
+    run_dns(N=N, Re=Re, K0=K0, STEPS=STEPS, CFL=CFL, start_spectrum=SPEC, UPDATE=UPDATE, method=METHOD,
+            precision=PREC)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,294 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle, through the C ABI.
+
+Tolerances (rel-L2 on the spectral vorticity om2 unless stated):
+  FP64 path vs FP64 oracle : 1e-12 after 100 steps (1e-13 after one step)
+  FP32 form vs FP64 oracle : 1e-4 after 100 steps
+Both paths start from the identical initial arrays (the reference generator's
+output, committed as fixtures) and compute their own CFL-adaptive dt; the dt
+sequences are compared as well.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import dns_oracle as do
+from oracle import pao_generator as pg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ts(built_lib):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from palinstrophy_gb300 import turbo_simulator
+    return turbo_simulator
+
+
+def _init(name):
+    d = golden(name)
+    return d["om2"], d["uc_low"], float(d["visc"])
+
+
+def _pair(ts, N, prec, om2, uc, visc, cfl):
+    F = ts.Field(N, prec, 1e4, cfl)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", visc)
+    F.set_scalar("cflnum", cfl)
+    S = do.OracleState(N, om2, uc, visc, cfl, dtype=np.float64)
+    return F, S
+
+
+def _gpu_init_dt(F):
+    F.step2a()
+    c = F.compute_cflm()
+    dt = F.scalars()["cflnum"] / (c * math.pi)
+    F.set_scalar("dt", dt)
+    F.set_scalar("cn", 1.0)
+    F.set_scalar("cnm1", 0.0)
+    F.set_scalar("t", 0.0)
+    F.set_scalar("it", 0)
+    return c
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
+@pytest.mark.parametrize("N,init", [(64, "init_KM3_N64_s4895_k10.npz"), (256, "init_KM3_N256_s4895_k10.npz")])
+def test_initial_physical_field(ts, prec, tol, N, init):
+    om2, uc, visc = _init(init)
+    F, S = _pair(ts, N, prec, om2, uc, visc, 0.75)
+    F.step2a()
+    do.step2a(S)
+    for c in (0, 1):
+        ref = S.ur_full[c]
+        got = F.ur(c).astype(np.float64)
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < tol
+    c_gpu, c_ref = F.compute_cflm(), do.compute_cflm(S)
+    assert abs(c_gpu - c_ref) <= tol * c_ref
+    F.close()
+
+
+def _run_pair(ts, N, prec, init, cfl, method, steps, update):
+    om2, uc, visc = _init(init)
+    F, S = _pair(ts, N, prec, om2, uc, visc, cfl)
+    c0g = _gpu_init_dt(F)
+    c0 = do.init_dt(S)
+    log = []
+    do.run(S, steps, method, update, log=log)
+    F.step(method, steps, update=update, final_update=True)
+    return F, S, c0g, c0, log
+
+
+@pytest.mark.parametrize("method,N,init,cfl,update", [
+    ("CNAB2", 256, "init_KM3_N256_s4895_k10.npz", 0.75, 10),
+    ("LS_IMEX_RK3", 128, "init_PAO_N128_s4895_k15.npz", 0.1, 25),
+    ("CNAB2", 64, "init_KM3_N64_s4895_k10.npz", 0.75, 7),
+])
+def test_fp64_parity_100_steps(ts, method, N, init, cfl, update):
+    F, S, c0g, c0, log = _run_pair(ts, N, "fp64", init, cfl, method, 100, update)
+    assert abs(c0g - c0) <= 1e-14 * c0
+    err_om = do.rel_l2(S.om2, F.om2())
+    err_fn = do.rel_l2(S.fnm1, F.fnm1())
+    sc = F.scalars()
+    assert err_om <= 1e-12, err_om
+    assert err_fn <= 1e-10, err_fn
+    assert abs(sc["dt"] - S.dt) <= 1e-13 * S.dt
+    assert abs(sc["cn"] - S.cn) <= 1e-13
+    assert abs(sc["t"] - S.t) <= 1e-13 * S.t
+    assert sc["it"] == 100
+    F.close()
+
+
+@pytest.mark.parametrize("method,N,init,cfl,update", [
+    ("CNAB2", 256, "init_KM3_N256_s4895_k10.npz", 0.75, 10),
+    ("LS_IMEX_RK3", 128, "init_PAO_N128_s4895_k15.npz", 0.1, 25),
+])
+def test_fp32_form_within_1e4(ts, method, N, init, cfl, update):
+    F, S, _, _, _ = _run_pair(ts, N, "fp32", init, cfl, method, 100, update)
+    err = do.rel_l2(S.om2, F.om2())
+    assert err <= 1e-4, err
+    assert abs(F.scalars()["dt"] - S.dt) <= 1e-5 * S.dt
+    F.close()
+
+
+def test_fp32_against_reference_fixture(ts):
+    """FP32 form against the reference's own FP32 CPU run (fixture)."""
+    d = golden("run_CNAB2_N256_s4895.npz")
+    F = ts.Field(256, "fp32", 1e4, 0.75)
+    F.set_state(d["om2_0"], None, d["uc_low_0"])
+    F.set_scalar("visc", float(d["visc"]))
+    _gpu_init_dt(F)
+    F.step("CNAB2", 100, update=100, final_update=True)
+    assert do.rel_l2(d["om2_100"], F.om2()) <= 1e-4
+    F.close()
+
+
+def test_diagnostics_match_oracle(ts):
+    om2, uc, visc = _init("init_KM3_N256_s4895_k10.npz")
+    F, S = _pair(ts, 256, "fp64", om2, uc, visc, 0.75)
+    _gpu_init_dt(F)
+    do.init_dt(S)
+    F.step("CNAB2", 5, update=0)
+    for _ in range(5):
+        do.cnab2(S)
+    d = F.diagnostics()
+    U, Lh, tau = do.flow_eddy_metrics(S)
+    sp = do.spectral_sums(S)
+    assert abs(d["U"] - U) <= 1e-12 * U
+    assert abs(d["L"] - Lh) <= 1e-12 * Lh
+    assert abs(d["tau_l"] - tau) <= 1e-12 * tau
+    for k in ("E", "Z", "P", "kmax2", "pal_over_ens_kmax2"):
+        assert abs(d[k] - sp[k]) <= 1e-12 * abs(sp[k]), k
+    assert abs(d["energy_joules"] - do.energy_joules(S)) <= 1e-12 * do.energy_joules(S)
+    assert d["nonfinite"] == 0
+    F.close()
+
+
+@pytest.mark.parametrize("method", ["CNAB2", "LS_IMEX_RK3"])
+def test_split_api_equals_fused_loop(ts, method):
+    """dns_step2b/dns_step3/dns_step2a + next_dt == the fused pal_step loop, bit for bit."""
+    om2, uc, visc = _init("init_KM3_N64_s4895_k10.npz")
+    A = ts.Field(64, "fp64", 1e4, 0.5)
+    B = ts.Field(64, "fp64", 1e4, 0.5)
+    for F in (A, B):
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", visc)
+        _gpu_init_dt(F)
+    A.step(method, 20, update=5, final_update=True)
+    for it in range(1, 21):
+        if method == "CNAB2":
+            B.step2b()
+            B.step3()
+            B.step2a()
+        else:
+            B.step_rk3()
+        if it % 5 == 0 or it == 1:
+            B.next_dt(sync_host=False)
+    assert np.array_equal(A.om2(), B.om2())
+    assert np.array_equal(A.fnm1(), B.fnm1())
+    sa, sb = A.scalars(), B.scalars()
+    assert sa["dt"] == sb["dt"] and sa["cn"] == sb["cn"]
+    A.close()
+    B.close()
+
+
+SMALL = [32, 64, 128, 256, 384, 512, 768, 1024]
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 5e-6)])
+@pytest.mark.parametrize("N", SMALL)
+def test_every_small_size_against_oracle(ts, prec, tol, N):
+    """Every radix plan up to N=1024: 3 RK3 steps against the oracle."""
+    g = pg.generate(N, 8.0, 1e4, 11, "KM3") if N <= 256 else None
+    if g is None:
+        from palinstrophy_gb300 import _lib as L
+        om2, uc, st = L.pao_generate(N, 8.0, 1e4, 11, "KM3")
+        visc = st["visc"]
+    else:
+        om2, uc, visc = g["om2"], g["uc_low"], float(g["visc"])
+    F, S = _pair(ts, N, prec, om2, uc, visc, 0.3)
+    _gpu_init_dt(F)
+    do.init_dt(S)
+    F.step("LS_IMEX_RK3", 3, update=1, final_update=True)
+    do.run(S, 3, "LS_IMEX_RK3", update=1)
+    assert do.rel_l2(S.om2, F.om2()) <= tol
+    F.close()
+
+
+@pytest.mark.parametrize("N", [2048, 3072, 4096])
+def test_large_sizes_fp32_vs_fp64(ts, N):
+    """Above the oracle's comfortable range: the FP32 and FP64 plans (different
+    radix orders) must agree to FP32 accuracy, and the step must conserve the
+    Parseval identity between physical and spectral energy."""
+    from palinstrophy_gb300 import _lib as L
+    om2, uc, st = L.pao_generate(N, 15.0, 1e5, 4895, "KM3")
+    out = {}
+    for prec in ("fp64", "fp32"):
+        F = ts.Field(N, prec, 1e5, 0.1)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        _gpu_init_dt(F)
+        F.step("LS_IMEX_RK3", 2, update=1, final_update=True)
+        out[prec] = (F.om2().astype(np.complex128), F.diagnostics())
+        F.close()
+    assert do.rel_l2(out["fp64"][0], out["fp32"][0]) <= 2e-5
+    d = out["fp64"][1]
+    om = out["fp64"][0]
+    nh = N // 2
+    kx = np.arange(nh)[None, :]
+    kz = np.fft.fftfreq(N, 1.0 / N)[:, None]
+    k2 = kx * kx + kz * kz
+    w = np.where(kx == 0, 1.0, 2.0)
+    spec = float((w * np.abs(om) ** 2 / np.where(k2 > 0, k2, 1.0) * (k2 > 0)).sum())
+    assert abs(d["U"] ** 2 - spec) <= 1e-6 * spec
+
+
+def test_fp32_largest_grid_runs(ts):
+    from palinstrophy_gb300 import _lib as L
+    N = 8192
+    om2, uc, st = L.pao_generate(N, 15.0, 1e5, 4895, "KM3")
+    F = ts.Field(N, "fp32", 1e5, 0.1)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", st["visc"])
+    _gpu_init_dt(F)
+    e0 = F.diagnostics()
+    F.step("LS_IMEX_RK3", 2, update=1, final_update=True)
+    e1 = F.diagnostics()
+    assert e1["nonfinite"] == 0
+    assert 0.9 * e0["U"] < e1["U"] <= 1.0001 * e0["U"]
+    F.close()
+
+
+def test_call_order_is_enforced(ts):
+    from palinstrophy_gb300 import _lib as L
+    om2, uc, visc = _init("init_KM3_N64_s4895_k10.npz")
+    F = ts.Field(64, "fp32", 1e4, 0.5)
+    with pytest.raises(L.PalError):
+        F.step2b()  # no state yet
+    F.set_state(om2, None, uc)
+    with pytest.raises(L.PalError):
+        F.step3()  # needs step2b first
+    F.step2b()
+    with pytest.raises(L.PalError):
+        F.step2a()  # between step2b and step3
+    F.step3()
+    F.close()
+
+
+def test_nonfinite_input_is_flagged(ts):
+    om2, uc, visc = _init("init_KM3_N64_s4895_k10.npz")
+    bad = om2.copy()
+    bad[3, 4] = np.nan
+    F = ts.Field(64, "fp64", 1e4, 0.5)
+    F.set_state(bad, None, None)
+    d = F.diagnostics()
+    assert d["nonfinite"] == 1
+    F.close()
+
+
+def test_velocity_rebuilt_from_om2(ts):
+    """Without uc_low the first step2a inverts om2 (restart path); it must match the
+    generator's velocity to rounding, since both describe the same field."""
+    om2, uc, visc = _init("init_KM3_N64_s4895_k10.npz")
+    A = ts.Field(64, "fp64", 1e4, 0.5)
+    A.set_state(om2, None, uc)
+    B = ts.Field(64, "fp64", 1e4, 0.5)
+    B.set_state(om2, None, None)
+    A.step2a()
+    B.step2a()
+    ua, ub = A.ur(0), B.ur(0)
+    assert np.linalg.norm(ua - ub) / np.linalg.norm(ua) < 1e-6
+    A.close()
+    B.close()
+
+
+def test_dropin_run_dns(ts, capsys):
+    S = ts.run_dns(N=64, Re=1e4, K0=10.0, STEPS=21, CFL=0.75, start_spectrum="KM3", UPDATE=10,
+                   method="CNAB2", precision="fp64")
+    out = capsys.readouterr().out
+    assert "ITERATION     21" in out and "FPS" in out
+    assert S.it == 21
+    U, Lh, tau = S.flow_eddy_metrics()
+    assert U > 0 and Lh > 0 and tau > 0

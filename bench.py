@@ -1,0 +1,375 @@
+"""Benchmark: DNS steps/s at N=4096, FP32 form vs FP64 plain, on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload (the large single-field configuration): N=4096 (3/2-padded 6144^2),
+KM3 start K0=15 seed 4895, Re=1e5, LS-IMEX-RK3, CFL 0.1, synthetic initial
+field from the package's host generator.  One "step" is one full 3-stage
+LS-IMEX-RK3 step of the field (6 kernel launches).
+
+Printed JSON line (rank 0):
+  value      FP32-form steps/s, whole job (N ranks x replicas), device-timed with
+             CUDA events on the handle's stream, state resident in HBM; the
+             state (0.67 GB) is larger than L2, so no flush is needed.
+  fp64       the plain FP64 path on the same GPU and workload
+  e2e        the same metric through the C ABI from pinned host buffers: upload
+             of the initial om2 + velocity band, initial NEXTDT, K steps with the
+             run_dns NEXTDT cadence (host reads CFLM/dt at each update), and the
+             download of the final om2, all inside the timed region
+  roofline   the dominant kernel: algorithmic bytes per launch / its average
+             launch duration (events between launches on the same stream), against
+             MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline  the FP32 CPU port of the reference path (scipy.fft, the
+             reference's worker count) timed on this host for a bounded sample
+
+--impl reference times the reference's CPU implementation of the path (its FP32
+NumPy/scipy.fft step, restated operation for operation in oracle/ because the
+Python reference cannot be installed on the GPU host) on the same workload,
+with all host threads, for a bounded number of steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import platform
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_GRID = 4096
+K0, SEED, RE, CFL = 15.0, 4895, 1e5, 0.1
+METHOD = "LS_IMEX_RK3"
+UPDATE = 100
+METRIC = "DNS steps/s at N=4096: FP32 form vs FP64 plain, same GB300, ω relL2≤1e-4"
+WORKLOAD = ("DNS N=4096 (3/2-padded 6144^2) KM3 K0=15 seed 4895 Re=1e5 LS-IMEX-RK3 CFL 0.1, "
+            "FP32 form (FP64 dt/CFL/diagnostic scalars)")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = sorted(float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel, prec):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{prec}_N{N_GRID}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith("dram_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def _init_arrays():
+    from palinstrophy_gb300 import _lib as L
+    return L.pao_generate(N_GRID, K0, RE, SEED, "KM3")
+
+
+def _field(prec, om2, uc, visc):
+    from palinstrophy_gb300.turbo_simulator import Field
+    F = Field(N_GRID, prec, RE, CFL)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", visc)
+    F.step2a()
+    c0 = F.compute_cflm()
+    F.set_scalar("dt", CFL / (c0 * math.pi))
+    F.set_scalar("cn", 1.0)
+    F.set_scalar("cnm1", 0.0)
+    return F
+
+
+def _timed_steps(F, steps, warmup, sampler_index=None):
+    import torch
+    s = torch.cuda.ExternalStream(F.stream_ptr())
+    F.step(METHOD, warmup, update=UPDATE)
+    F.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(sampler_index) if sampler_index is not None else None
+    if clocks:
+        clocks.__enter__()
+        time.sleep(0.3)
+    e0.record(s)
+    F.step(METHOD, steps, update=UPDATE)
+    e1.record(s)
+    e1.synchronize()
+    if clocks:
+        clocks.__exit__()
+    return e0.elapsed_time(e1), (clocks.summary() if clocks else None)
+
+
+def _e2e(prec, om2, uc, visc, steps):
+    """Whole job through the C ABI from pinned host buffers (run_dns shape)."""
+    import numpy as np
+    import torch
+    from palinstrophy_gb300.turbo_simulator import Field
+    cdt = np.complex64 if prec == "fp32" else np.complex128
+    pin_om = torch.empty(om2.size * 2, dtype=torch.float32 if prec == "fp32" else torch.float64).pin_memory()
+    pin_uc = torch.empty(uc.size * 2, dtype=pin_om.dtype).pin_memory()
+    pin_out = torch.empty_like(pin_om).pin_memory()
+    h_om = pin_om.numpy().view(cdt).reshape(om2.shape)
+    h_uc = pin_uc.numpy().view(cdt).reshape(uc.shape)
+    h_out = pin_out.numpy().view(cdt).reshape(om2.shape)
+    h_om[...] = om2
+    h_uc[...] = uc
+    F = Field(N_GRID, prec, RE, CFL)
+    F.synchronize()
+    t0 = time.perf_counter()
+    F.set_state(h_om, None, h_uc)
+    F.set_scalar("visc", visc)
+    F.step2a()
+    c0 = F.compute_cflm()
+    F.set_scalar("dt", CFL / (c0 * math.pi))
+    F.set_scalar("cn", 1.0)
+    F.set_scalar("cnm1", 0.0)
+    marks = sorted({1, steps} | set(range(UPDATE, steps + 1, UPDATE)))
+    done = 0
+    for m in marks:
+        F.step(METHOD, m - done)
+        done = m
+        F.next_dt(sync_host=True)  # host reads CFLM/dt as run_dns does
+    F._ck(F.lib.pal_get_field(F.h, 0, h_out.ctypes.data_as(__import__("ctypes").c_void_p)))
+    t1 = time.perf_counter()
+    F.close()
+    esz = 8 if prec == "fp32" else 16
+    h2d = (om2.size + uc.size) * esz
+    d2h = om2.size * esz + len(marks) * 64
+    return steps / (t1 - t0), h2d / steps, d2h / steps
+
+
+def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
+    """FP32 CPU port of the reference path: steps/s over a bounded sample."""
+    import numpy as np
+    from oracle import dns_oracle as do
+    S = do.OracleState(N_GRID, om2, uc, visc, CFL, dtype=np.float32, workers=workers)
+    do.init_dt(S)
+    do.rk3(S)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while n < steps_cap and (time.perf_counter() - t0) < seconds:
+        do.rk3(S)
+        n += 1
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def _cpu_name():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part", "hardware")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    om2, uc, st = _init_arrays()
+    workers = os.cpu_count() or 1
+    rate, n, secs = _cpu_port_rate(max(1, args.steps), 90.0, workers, om2, uc, st["visc"])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": n, "warmup": 1, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (KM3 generator, seed 4895)",
+        "config": {"workload": WORKLOAD.replace("FP32 form (FP64 dt/CFL/diagnostic scalars)",
+                                                "reference FP32 CPU path (numpy + scipy.fft)"), "N": N_GRID},
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": workers, "kind": "port",
+                         "sample": f"{n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up step ({secs:.1f} s), "
+                                   f"scipy.fft workers={workers}, {_cpu_name()}"},
+        "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from oracle import dns_oracle as do
+    om2, uc, st = _init_arrays()
+    visc = st["visc"]
+
+    # FP32 form: headline
+    F = _field("fp32", om2, uc, visc)
+    ms_row, ms_col, _ = F.profile_kernels(METHOD, 3)
+    F.close()
+    F = _field("fp32", om2, uc, visc)
+    ms32, clocks = _timed_steps(F, args.steps, args.warmup, sampler_index=local)
+    F.close()
+    # FP64 plain path
+    k64 = max(3, args.steps // 40)
+    F = _field("fp64", om2, uc, visc)
+    ms64, _ = _timed_steps(F, k64, max(3, args.warmup // 10))
+    F.close()
+
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms32, ms64], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32, ms64 = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+
+    # accuracy: FP32 form vs FP64 plain after 100 steps from the identical start
+    A = _field("fp32", om2, uc, visc)
+    B = _field("fp64", om2, uc, visc)
+    A.step(METHOD, 100, update=UPDATE, final_update=True)
+    B.step(METHOD, 100, update=UPDATE, final_update=True)
+    rel = do.rel_l2(B.om2(), A.om2())
+    A.close()
+    B.close()
+
+    e2e_rate, h2d, d2h = _e2e("fp32", om2, uc, visc, args.steps)
+
+    rate32 = ws * args.steps / (ms32 / 1000.0)
+    rate64 = ws * k64 / (ms64 / 1000.0)
+    peak, peak_kind = _peaks()
+    s_bytes = 4
+    n2 = float(N_GRID) * N_GRID
+    bytes_row = 6.0 * n2 * s_bytes   # read + write 2 planes of (N/2 x 3N/2) complex
+    bytes_col = 10.0 * n2 * s_bytes  # the same + read/write om2 and fnm1 (N x N/2 complex)
+    dominant = "k_col" if ms_col >= ms_row else "k_row"
+    dom_ms = max(ms_col, ms_row)
+    dom_bytes = bytes_col if dominant == "k_col" else bytes_row
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
+    cpu_rate, cpu_n, cpu_s = _cpu_port_rate(3, 30.0, min(8, os.cpu_count() or 1), om2, uc, visc)
+    line = {
+        "metric": METRIC,
+        "value": rate32,
+        "unit": "steps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms32 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (KM3 generator, seed 4895)",
+        "config": {"workload": WORKLOAD, "N": N_GRID, "M": 3 * N_GRID // 2, "method": METHOD,
+                   "update": UPDATE, "l2": "state (0.67 GB FP32) larger than L2, no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "fp64": {"value": rate64, "unit": "steps/s", "steps": k64, "ms_per_step": ms64 / k64},
+        "fp32_over_fp64": rate32 / rate64,
+        "rel_l2_fp32_vs_fp64_100_steps": rel,
+        "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 6 * args.steps + (args.steps // UPDATE + 1),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": _traffic(dominant, "fp32"), "algorithmic_bytes": dom_bytes,
+                     "ms_per_launch": {"k_row": ms_row, "k_col": ms_col},
+                     "stage_bytes_per_s": (bytes_row + bytes_col) / ((ms_row + ms_col) / 1000.0) / 1e9},
+        "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": min(8, os.cpu_count() or 1),
+                         "kind": "port",
+                         "sample": f"{cpu_n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up ({cpu_s:.1f} s), FP32 "
+                                   f"numpy/scipy.fft port of the reference path, {_cpu_name()}"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
+                    help="profiling target: init + 2 warm-up + 2 timed steps of one precision, no JSON")
+    args = ap.parse_args()
+    if args.ncu_case:
+        om2, uc, st = _init_arrays()
+        F = _field(args.ncu_case, om2, uc, st["visc"])
+        F.step(METHOD, 2)
+        F.step(METHOD, 2)
+        F.synchronize()
+        F.close()
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

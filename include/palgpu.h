@@ -124,6 +124,12 @@ int pal_get_field(pal_handle* h, int which, void* host_dst);
 int pal_field_device_ptr(pal_handle* h, int which, void** ptr);
 int pal_materialize_physical(pal_handle* h);
 int pal_synchronize(pal_handle* h);
+/* Per-kernel timing: runs nsteps steps of `method` (no NEXTDT) with a CUDA
+ * event between consecutive launches on the handle's stream and returns the
+ * average duration of the row pass (k_row) and of the column pass (k_col) in
+ * milliseconds, and the number of kernels launched.  Measurement support; no
+ * counterpart in the reference. */
+int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, double* ms_col, int* launches);
 /* The handle's CUDA stream (cudaStream_t), for event timing or interop. */
 int pal_get_stream(pal_handle* h, void** stream);
 int pal_last_error(pal_handle* h, char* buf, size_t n);

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "palgpu.h"
 #include "pal_launch.cuh"
@@ -500,6 +501,60 @@ int pal_field_device_ptr(pal_handle* h, int which, void** ptr) {
 int pal_synchronize(pal_handle* h) {
   if (int rc = check(h)) return rc;
   PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, double* ms_col, int* launches) {
+  if (int rc = check(h)) return rc;
+  if (method != PAL_CNAB2 && method != PAL_LS_IMEX_RK3) return fail(h, PAL_ERR_INVALID, "unknown time stepper");
+  if (nsteps <= 0) return fail(h, PAL_ERR_INVALID, "nsteps must be positive");
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "profiling needs the physical velocity");
+  const int stages = method == PAL_CNAB2 ? 1 : 3;
+  const int n_ev = 2 * stages * nsteps + 1;
+  std::vector<cudaEvent_t> ev(n_ev, nullptr);
+  int rc = PAL_OK;
+  for (auto& e : ev) {
+    cudaError_t ce = cudaEventCreate(&e);
+    if (ce != cudaSuccess) {
+      rc = cuda_fail(h, ce, "cudaEventCreate");
+      break;
+    }
+  }
+  int k = 0;
+  if (rc == PAL_OK) {
+    cudaEventRecord(ev[k++], h->stream);
+    for (int j = 0; j < nsteps && rc == PAL_OK; ++j) {
+      for (int s = 0; s < stages && rc == PAL_OK; ++s) {
+        rc = launch_row(h, 0);
+        cudaEventRecord(ev[k++], h->stream);
+        if (rc == PAL_OK)
+          rc = launch_col(h, method == PAL_CNAB2 ? 0 : 1, s,
+                          (method == PAL_CNAB2 ? pal::F_CNM1 : 0) | (s == stages - 1 ? pal::F_ADVANCE : 0));
+        cudaEventRecord(ev[k++], h->stream);
+      }
+      if (rc == PAL_OK) h->it += 1;
+    }
+  }
+  double tr = 0.0, tc = 0.0;
+  if (rc == PAL_OK) {
+    cudaError_t ce = cudaEventSynchronize(ev[k - 1]);
+    if (ce != cudaSuccess) rc = cuda_fail(h, ce, "cudaEventSynchronize");
+    for (int q = 0; rc == PAL_OK && q + 2 <= k - 1; q += 2) {
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, ev[q], ev[q + 1]);
+      cudaEventElapsedTime(&b, ev[q + 1], ev[q + 2]);
+      tr += a;
+      tc += b;
+    }
+  }
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  if (rc != PAL_OK) return rc;
+  const int nl = stages * nsteps;
+  if (ms_row) *ms_row = tr / nl;
+  if (ms_col) *ms_col = tc / nl;
+  if (launches) *launches = 2 * nl;
   return PAL_OK;
 }
 

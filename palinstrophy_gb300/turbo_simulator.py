@@ -152,6 +152,13 @@ class Field:
     def synchronize(self):
         self._ck(self.lib.pal_synchronize(self.h))
 
+    def profile_kernels(self, method="LS_IMEX_RK3", nsteps=5):
+        """Average k_row / k_col launch durations (ms) from events on the handle stream."""
+        r, c, n = L._D(), L._D(), L._I()
+        self._ck(self.lib.pal_profile_kernels(self.h, _METHODS[method], int(nsteps), L.ctypes.byref(r),
+                                              L.ctypes.byref(c), L.ctypes.byref(n)))
+        return r.value, c.value, n.value
+
     def stream_ptr(self) -> int:
         p = L._P()
         self._ck(self.lib.pal_get_stream(self.h, L.ctypes.byref(p)))

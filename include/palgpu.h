@@ -134,6 +134,22 @@ int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, d
 int pal_get_stream(pal_handle* h, void** stream);
 int pal_last_error(pal_handle* h, char* buf, size_t n);
 
+/* Allocation-free stepping for callers that cannot allocate device memory at
+ * the point of the call (inside host callbacks or real-time loops that must not
+ * block on the allocator, plugins whose host forbids device allocations after
+ * start-up, tools that budget device memory up front).  No counterpart in the
+ * reference.  Advances a field given as caller-owned device arrays om2 and
+ * fnm1 ((N, N/2) complex64, reference layout, updated in place) by nsteps steps
+ * of `method` at fixed dt (no NEXTDT), with the velocity rebuilt from om2 first
+ * and cn/cnm1 the AB2 weights of the first CNAB2 step.  Work planes live in a
+ * 6 MiB scratch array inside the library (one per GPU, resident until exit):
+ * FP32 only and N <= 512, otherwise PAL_ERR_INVALID.  Nothing is allocated.
+ * Asynchronous on `stream`; calls whose GPU work overlaps share the scratch
+ * and race.  The first call on a device looks the scratch up and should come
+ * before any stream capture. */
+int pal_step_noalloc(int N, int method, int nsteps, double dt, double visc, double cn, double cnm1,
+                     void* om2, void* fnm1, void* stream);
+
 /* Host-side PAO / KM3 initial condition (turbo_simulator.py:213-485, 1059-1239,
  * 1314-1361), complex64 outputs: om2 (N, N/2) and uc_low (2, N, N/2).
  * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed. */

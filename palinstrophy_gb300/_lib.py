@@ -71,6 +71,7 @@ _SIGS = {
     "pal_get_stream": (_I, [_H, ctypes.POINTER(_P)]),
     "pal_profile_kernels": (_I, [_H, _I, _I, _DP, _DP, ctypes.POINTER(_I)]),
     "pal_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
+    "pal_step_noalloc": (_I, [_I, _I, _I, _D, _D, _D, _D, _P, _P, _P]),
     "pal_pao_generate": (_I, [_I, _D, _D, _I, _I, _P, _P, _DP, ctypes.POINTER(_I)]),
 }
 

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xc
               "-I" + INCLUDE, "-I" + CSRC] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE]
 
-CU_SOURCES = ["pal_inst_f32.cu", "pal_inst_f64.cu", "pal_api.cu"]
+CU_SOURCES = ["pal_inst_f32.cu", "pal_inst_f64.cu", "pal_api.cu", "pal_noalloc.cu"]
 CPP_SOURCES = ["pal_pao.cpp"]
 
 

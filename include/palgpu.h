@@ -130,6 +130,15 @@ int pal_synchronize(pal_handle* h);
  * milliseconds, and the number of kernels launched.  Measurement support; no
  * counterpart in the reference. */
 int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, double* ms_col, int* launches);
+/* Kernel candidates: for each N the library compiles several row-pass and
+ * column-pass kernels (radix order, rows per tile, threads per block).
+ * pal_create times them on the new handle and keeps the fastest, once per
+ * (precision, N) per process; PAL_AUTOTUNE=0 in the environment keeps the
+ * first candidates instead.  pal_get_variant reports the choice and a short
+ * description; pal_set_variant forces one (between steps).  Performance
+ * control; no counterpart in the reference. */
+int pal_get_variant(pal_handle* h, int* row, int* col, int* n_rows, int* n_cols, char* desc, size_t desc_len);
+int pal_set_variant(pal_handle* h, int row, int col);
 /* The handle's CUDA stream (cudaStream_t), for event timing or interop. */
 int pal_get_stream(pal_handle* h, void** stream);
 int pal_last_error(pal_handle* h, char* buf, size_t n);

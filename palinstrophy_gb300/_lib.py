@@ -69,6 +69,9 @@ _SIGS = {
     "pal_materialize_physical": (_I, [_H]),
     "pal_synchronize": (_I, [_H]),
     "pal_get_stream": (_I, [_H, ctypes.POINTER(_P)]),
+    "pal_get_variant": (_I, [_H, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                             ctypes.c_char_p, ctypes.c_size_t]),
+    "pal_set_variant": (_I, [_H, _I, _I]),
     "pal_profile_kernels": (_I, [_H, _I, _I, _DP, _DP, ctypes.POINTER(_I)]),
     "pal_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
     "pal_step_noalloc": (_I, [_I, _I, _I, _D, _D, _D, _D, _P, _P, _P]),

@@ -6,15 +6,21 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "palgpu.h"
 #include "pal_launch.cuh"
 
+using pal::ColKernels;
 using pal::DevScalars;
 using pal::KernelSet;
+using pal::RowKernels;
 using pal::StepArgs;
 
 namespace {
@@ -33,8 +39,12 @@ struct pal_handle {
   int N = 0, M = 0, Nh = 0, precision = 0;
   size_t esz = 0;  // bytes per complex element
   const KernelSet* ks = nullptr;
+  const RowKernels* rk = nullptr;  // selected row-pass candidate
+  const ColKernels* ck = nullptr;  // selected column-pass candidate
+  int row_idx = 0, col_idx = 0;
   cudaStream_t stream = nullptr;
-  void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr, *tw = nullptr;
+  void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
+  void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
   DevScalars* sc = nullptr;
   DevScalars* sc_host = nullptr;  // pinned mirror
@@ -78,7 +88,7 @@ StepArgs base_args(pal_handle* h) {
   a.w1 = h->w1;
   a.om = h->om;
   a.fnm1 = h->fnm1;
-  a.tw = h->tw;
+  a.tw = h->tw_row;
   a.sc = h->sc;
   a.part = h->part;
   a.phys = h->phys;
@@ -86,28 +96,13 @@ StepArgs base_args(pal_handle* h) {
   return a;
 }
 
-// Forward twiddles exp(-2 pi i m / M), evaluated in extended precision and
-// rounded once to the working precision.
-void make_twiddles(int M, int precision, void* host) {
-  for (int m = 0; m < M; ++m) {
-    const long double ang = 2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)M;
-    const double c = (double)cosl(ang), s = (double)-sinl(ang);
-    if (precision == PAL_FP64) {
-      static_cast<double*>(host)[2 * m] = c;
-      static_cast<double*>(host)[2 * m + 1] = s;
-    } else {
-      static_cast<float*>(host)[2 * m] = (float)c;
-      static_cast<float*>(host)[2 * m + 1] = (float)s;
-    }
-  }
-}
-
 int resolve_velocity(pal_handle* h) {
   if (h->state == ST_EMPTY) return fail(h, PAL_ERR_STATE, "no spectral state set");
   if (h->state != ST_VEL_PENDING) return PAL_OK;
   StepArgs a = base_args(h);
+  a.tw = h->tw_col;
   a.src = h->vel_uploaded ? h->stage : nullptr;
-  h->ks->col_inv(a, h->stream);
+  h->ck->col_inv(a, h->stream);
   PAL_LAUNCHED(h, "k_col_inv");
   h->state = ST_U;
   h->vel_uploaded = false;
@@ -117,7 +112,7 @@ int resolve_velocity(pal_handle* h) {
 int launch_row(pal_handle* h, int flags) {
   StepArgs a = base_args(h);
   a.flags = flags;
-  h->ks->row(a, h->stream);
+  h->rk->row(a, h->stream);
   PAL_LAUNCHED(h, "k_row");
   h->state = ST_P;
   return PAL_OK;
@@ -125,13 +120,14 @@ int launch_row(pal_handle* h, int flags) {
 
 int launch_col(pal_handle* h, int scheme, int stage, int flags) {
   StepArgs a = base_args(h);
+  a.tw = h->tw_col;
   a.flags = flags;
   a.scheme = scheme;
   if (scheme == 1) {
     a.alpha = kRkAlpha[stage];
     a.beta = kRkBeta[stage];
   }
-  h->ks->col(a, h->stream);
+  h->ck->col(a, h->stream);
   PAL_LAUNCHED(h, "k_col");
   h->state = ST_U;
   return PAL_OK;
@@ -143,7 +139,7 @@ int launch_phys(pal_handle* h, int flags) {
   if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "physical field requested between step2b and step3");
   StepArgs a = base_args(h);
   a.flags = flags | pal::F_STATS;
-  h->ks->phys(a, h->stream);
+  h->rk->phys(a, h->stream);
   PAL_LAUNCHED(h, "k_phys");
   return PAL_OK;
 }
@@ -172,6 +168,92 @@ int one_step(pal_handle* h, int method, bool dt_update, bool advance) {
 int check(pal_handle* h) {
   if (!h) return fail(nullptr, PAL_ERR_INVALID, "null handle");
   return PAL_OK;
+}
+
+// Select candidates and (re)build their twiddle tables.
+int select_variant(pal_handle* h, int row, int col) {
+  if (row < 0 || row >= h->ks->n_rows || col < 0 || col >= h->ks->n_cols)
+    return fail(h, PAL_ERR_INVALID, "variant index out of range");
+  h->row_idx = row;
+  h->col_idx = col;
+  h->rk = &h->ks->rows[row];
+  h->ck = &h->ks->cols[col];
+  h->rk->twiddles(h->tw_row, h->stream);
+  h->ck->twiddles(h->tw_col, h->stream);
+  PAL_LAUNCHED(h, "twiddle tables");
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  return PAL_OK;
+}
+
+// Process-wide choice per (precision, N), so every handle of a size runs the
+// same kernels (and gives bit-identical results).
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, std::pair<int, int>> g_tuned;
+
+// Time every candidate on the handle's (still zero) state and keep the fastest.
+// The kernels' cost does not depend on the values they transform.
+int autotune(pal_handle* h) {
+  const auto key = std::make_pair(h->precision, h->N);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) return select_variant(h, it->second.first, it->second.second);
+  }
+  const char* env = std::getenv("PAL_AUTOTUNE");
+  int best_row = 0, best_col = 0;
+  if (!(env && env[0] == '0') && (h->ks->n_rows > 1 || h->ks->n_cols > 1)) {
+    cudaEvent_t e0, e1;
+    PAL_CK(h, cudaEventCreate(&e0));
+    PAL_CK(h, cudaEventCreate(&e1));
+    const int reps = 4;
+    float best = 1e30f;
+    for (int r = 0; r < h->ks->n_rows; ++r) {
+      if (int rc = select_variant(h, r, 0)) return rc;
+      StepArgs a = base_args(h);
+      h->rk->row(a, h->stream);  // warm-up
+      cudaEventRecord(e0, h->stream);
+      for (int q = 0; q < reps; ++q) h->rk->row(a, h->stream);
+      cudaEventRecord(e1, h->stream);
+      PAL_LAUNCHED(h, "autotune k_row");
+      PAL_CK(h, cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_row = r;
+      }
+    }
+    best = 1e30f;
+    for (int c = 0; c < h->ks->n_cols; ++c) {
+      if (int rc = select_variant(h, 0, c)) return rc;
+      StepArgs a = base_args(h);
+      a.tw = h->tw_col;
+      a.scheme = 1;
+      h->ck->col(a, h->stream);
+      cudaEventRecord(e0, h->stream);
+      for (int q = 0; q < reps; ++q) h->ck->col(a, h->stream);
+      cudaEventRecord(e1, h->stream);
+      PAL_LAUNCHED(h, "autotune k_col");
+      PAL_CK(h, cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_col = c;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // leave the work planes as a fresh handle has them
+    const size_t plane_w = (size_t)h->Nh * h->M * h->esz;
+    PAL_CK(h, cudaMemsetAsync(h->w0, 0, plane_w, h->stream));
+    PAL_CK(h, cudaMemsetAsync(h->w1, 0, plane_w, h->stream));
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tuned[key] = std::make_pair(best_row, best_col);
+  }
+  return select_variant(h, best_row, best_col);
 }
 
 }  // namespace
@@ -218,7 +300,16 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
     pal_destroy(h);
     return code;
   };
-  cudaError_t e = ks->configure();
+  cudaError_t e = cudaSuccess;
+  size_t tw_max = 0;
+  for (int r = 0; r < ks->n_rows && e == cudaSuccess; ++r) {
+    e = ks->rows[r].configure();
+    tw_max = std::max(tw_max, (size_t)ks->rows[r].tw_elems);
+  }
+  for (int c = 0; c < ks->n_cols && e == cudaSuccess; ++c) {
+    e = ks->cols[c].configure();
+    tw_max = std::max(tw_max, (size_t)ks->cols[c].tw_elems);
+  }
   if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "kernel configure"));
   e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaStreamCreate"));
@@ -229,9 +320,9 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   h->spectral_blocks = std::max(1, std::min(4 * sms, (int)(((size_t)N * h->Nh + 255) / 256)));
   const size_t part_n = (size_t)std::max(h->M, std::max(1024, h->spectral_blocks)) * 5;
-  void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw};
-  const size_t sizes[] = {plane_w, plane_w, plane_om, plane_om, 2 * plane_om, (size_t)h->M * h->esz};
-  for (int i = 0; i < 6; ++i) {
+  void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw_row, &h->tw_col};
+  const size_t sizes[] = {plane_w, plane_w, plane_om, plane_om, 2 * plane_om, tw_max * h->esz, tw_max * h->esz};
+  for (int i = 0; i < 7; ++i) {
     e = cudaMalloc(bufs[i], sizes[i]);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc state"));
     e = cudaMemsetAsync(*bufs[i], 0, sizes[i], h->stream);
@@ -249,12 +340,11 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
   h->sc_host->cflnum = cfl;
   e = cudaMemcpyAsync(h->sc, h->sc_host, sizeof(DevScalars), cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "upload scalars"));
-  {
-    std::string tw((size_t)h->M * h->esz, '\0');
-    make_twiddles(h->M, precision, &tw[0]);
-    e = cudaMemcpyAsync(h->tw, tw.data(), tw.size(), cudaMemcpyHostToDevice, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "upload twiddles"));
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "initialise state"));
+  if (int rc = autotune(h)) {
+    g_err = h->err;
+    return bail(rc);
   }
   *out = h;
   return PAL_OK;
@@ -263,7 +353,7 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
 int pal_destroy(pal_handle* h) {
   if (!h) return PAL_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* bufs[] = {h->w0, h->w1, h->om, h->fnm1, h->stage, h->tw, h->phys, h->sc, h->part};
+  void* bufs[] = {h->w0, h->w1, h->om, h->fnm1, h->stage, h->tw_row, h->tw_col, h->phys, h->sc, h->part};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -556,6 +646,24 @@ int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, d
   if (ms_col) *ms_col = tc / nl;
   if (launches) *launches = 2 * nl;
   return PAL_OK;
+}
+
+int pal_get_variant(pal_handle* h, int* row, int* col, int* n_rows, int* n_cols, char* desc, size_t desc_len) {
+  if (int rc = check(h)) return rc;
+  if (row) *row = h->row_idx;
+  if (col) *col = h->col_idx;
+  if (n_rows) *n_rows = h->ks->n_rows;
+  if (n_cols) *n_cols = h->ks->n_cols;
+  if (desc && desc_len) {
+    std::snprintf(desc, desc_len, "row[%s] col[%s]", h->rk->name, h->ck->name);
+  }
+  return PAL_OK;
+}
+
+int pal_set_variant(pal_handle* h, int row, int col) {
+  if (int rc = check(h)) return rc;
+  if (h->state == ST_P) return fail(h, PAL_ERR_STATE, "change kernels between steps, not between step2b and step3");
+  return select_variant(h, row, col);
 }
 
 int pal_get_stream(pal_handle* h, void** stream) {

@@ -182,6 +182,15 @@ struct Plan {
   }
   static constexpr int PADM = M + M / RP;
   static __device__ __forceinline__ int phys(int k) { return k + k / RP; }
+  // physical slot stride of pass p (every stride but the last is a multiple of RP)
+  static constexpr int pstride(int p) { return stride(p) == 1 ? 1 : stride(p) + stride(p) / RP; }
+  // twiddle tables: pass p holds W_{L_p}^(i k) as [i][k], i < S_p, k < R_p
+  static constexpr int tw_off(int p) {
+    int o = 0;
+    for (int q = 0; q < p; ++q) o += stride(q) * R[q];
+    return o;
+  }
+  static constexpr int TW_TOTAL = tw_off(NP);
   // frequency index of the DIF output stored at position pos (every constant
   // is a template-time value, so no radix table is touched at run time)
   template <int Q>
@@ -202,12 +211,43 @@ struct Plan {
   }
 };
 
-// Twiddle W_M^(SIGN*m) from the forward table tw[m] = exp(-2 pi i m / M).
+// x * W^(SIGN) where w = exp(-2 pi i e / L) is a forward-table entry.
 template <int SIGN, typename C>
-__device__ __forceinline__ C twl(const C* __restrict__ tw, int m) {
-  C w = __ldg(tw + m);
-  if constexpr (SIGN > 0) w.y = -w.y;
-  return w;
+__device__ __forceinline__ C twmul(C x, C w) {
+  if constexpr (SIGN > 0) {
+    return cmulc(x, w);
+  } else {
+    return cmul(x, w);
+  }
+}
+
+// The R twiddles of butterfly i of a pass, as 128-bit loads (row i of the table).
+template <int R>
+__device__ __forceinline__ void load_tw(const float2* __restrict__ t, float2 (&w)[R]) {
+  static_assert(R % 2 == 0, "even radix");
+#pragma unroll
+  for (int q = 0; q < R / 2; ++q) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(t) + q);
+    w[2 * q] = make_float2(v.x, v.y);
+    w[2 * q + 1] = make_float2(v.z, v.w);
+  }
+}
+template <int R>
+__device__ __forceinline__ void load_tw(const double2* __restrict__ t, double2 (&w)[R]) {
+#pragma unroll
+  for (int q = 0; q < R; ++q) w[q] = __ldg(t + q);
+}
+template <int R, int SIGN, typename C>
+__device__ __forceinline__ void apply_tw(C (&x)[R], const C* __restrict__ t) {
+  if constexpr (R % 2 == 0 && sizeof(C) == 8) {  // FP32: pairs of twiddles per 128-bit load
+    C w[R];
+    load_tw<R>(t, w);
+#pragma unroll
+    for (int k = 1; k < R; ++k) x[k] = twmul<SIGN>(x[k], w[k]);
+  } else {
+#pragma unroll
+    for (int k = 1; k < R; ++k) x[k] = twmul<SIGN>(x[k], __ldg(t + k));
+  }
 }
 
 // One DIF pass p over a [slot][v] tile in shared memory.
@@ -217,24 +257,21 @@ __device__ __forceinline__ void dif_pass(cplx<T>* sm, const cplx<T>* __restrict_
   constexpr int R = PL::R[P];
   constexpr int L = PL::span(P);
   constexpr int S = L / R;
+  constexpr int SP = PL::pstride(P);
   constexpr int NB = V * (PL::M / R);
-  constexpr int TS = PL::M / L;  // twiddle table step
   for (int w = tid; w < NB; w += NT) {
     const int v = w % V;
     const int b = w / V;
     const int blk = b / S;
     const int i = b - blk * S;
-    const int base = blk * L + i;
+    C* p = sm + PL::phys(blk * L + i) * V + v;
     C x[R];
 #pragma unroll
-    for (int j = 0; j < R; ++j) x[j] = sm[PL::phys(base + j * S) * V + v];
+    for (int j = 0; j < R; ++j) x[j] = p[j * SP * V];
     Dft<R, SIGN, C>::run(x);
-    if constexpr (S > 1) {
+    if constexpr (S > 1) apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
 #pragma unroll
-      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<SIGN>(tw, TS * i * k));
-    }
-#pragma unroll
-    for (int k = 0; k < R; ++k) sm[PL::phys(base + k * S) * V + v] = x[k];
+    for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
   }
 }
 
@@ -245,25 +282,50 @@ __device__ __forceinline__ void dit_pass(cplx<T>* sm, const cplx<T>* __restrict_
   constexpr int R = PL::R[P];
   constexpr int L = PL::span(P);
   constexpr int S = L / R;
+  constexpr int SP = PL::pstride(P);
   constexpr int NB = V * (PL::M / R);
-  constexpr int TS = PL::M / L;
   for (int w = tid; w < NB; w += NT) {
     const int v = w % V;
     const int b = w / V;
     const int blk = b / S;
     const int i = b - blk * S;
-    const int base = blk * L + i;
+    C* p = sm + PL::phys(blk * L + i) * V + v;
     C x[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) x[k] = sm[PL::phys(base + k * S) * V + v];
-    if constexpr (S > 1) {
-#pragma unroll
-      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<SIGN>(tw, TS * i * k));
-    }
+    for (int k = 0; k < R; ++k) x[k] = p[k * SP * V];
+    if constexpr (S > 1) apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
     Dft<R, SIGN, C>::run(x);
 #pragma unroll
-    for (int j = 0; j < R; ++j) sm[PL::phys(base + j * S) * V + v] = x[j];
+    for (int j = 0; j < R; ++j) p[j * SP * V] = x[j];
   }
+}
+
+// Angle (in units of pi) of table entry e: W_{L_p}^(i k) = exp(-2 pi i (M/L_p) i k / M).
+template <class PL, int Q>
+__device__ __forceinline__ double tw_angle(int e) {
+  if constexpr (Q < PL::NP) {
+    constexpr int off = PL::tw_off(Q);
+    constexpr int R = PL::R[Q];
+    constexpr int S = PL::stride(Q);
+    constexpr int step = PL::M / PL::span(Q);
+    if (e < off + S * R) {
+      const int i = (e - off) / R;
+      const int k = (e - off) - i * R;
+      return 2.0 * (double)((long long)step * i * k) / (double)PL::M;
+    }
+    return tw_angle<PL, Q + 1>(e);
+  }
+  return 0.0;
+}
+
+// Fill every pass table, evaluated in double and rounded once to T.
+template <typename T, class PL>
+__global__ void k_twiddles(cplx<T>* tw) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= PL::TW_TOTAL) return;
+  double sn, cs;
+  sincospi(tw_angle<PL, 0>(e), &sn, &cs);
+  tw[e] = cplx<T>{T(cs), T(-sn)};
 }
 
 // DIF passes FROM..TO-1 (each followed by a barrier).

@@ -171,7 +171,7 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
   const C* __restrict__ w0 = static_cast<const C*>(a.w0);
   const C* __restrict__ w1 = static_cast<const C*>(a.w1);
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
-  const int Nh = a.N >> 1;
+  constexpr int Nh = M / 3;
   for (int w = tid; w < V * S; w += NT) {
     const int v = w % V;
     const int i = w / V;
@@ -181,7 +181,9 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
     for (int j = 0; j < R; ++j) {
       const int k = i + j * S;
       C zz = {T(0), T(0)};
-      if (k < Nh) {
+      if (j * S >= Nh && j * S + S - 1 <= M - Nh) {
+        // whole row segment inside the 3/2 pad: zero
+      } else if (k < Nh) {
         const C u = w0[(size_t)k * M + z];
         const C q = w1[(size_t)k * M + z];
         zz = (k == 0) ? C{u.x, q.x} : C{u.x - q.y, u.y + q.x};
@@ -194,12 +196,76 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
       x[j] = zz;
     }
     Dft<R, +1, C>::run(x);
+    apply_tw<R, +1>(x, tw + i * R);
+    C* p = sm + PL::phys(i) * V + v;
 #pragma unroll
-    for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<+1>(tw, i * k));
-#pragma unroll
-    for (int k = 0; k < R; ++k) sm[PL::phys(i + k * S) * V + v] = x[k];
+    for (int k = 0; k < R; ++k) p[k * PL::pstride(0) * V] = x[k];
   }
   __syncthreads();
+}
+
+// Last forward DIT pass of the row kernel fused with the Hermitian unpack.
+// Butterfly i produces P[i + j S]; the conjugate partner P[M - i - j S] sits in
+// butterfly S - i at index R-1-j (or, for i = 0, in butterfly 0 at (R-j) mod R),
+// so one thread transforms the pair (i, S - i) and writes
+// A = (P[k] + conj P[M-k]) / 2 and B = (P[k] - conj P[M-k]) / (2i) for k < N/2
+// straight to the work planes.  Outputs with N/2 <= k <= M - N/2 are never formed.
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>* sm, int z0, int tid) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  constexpr int SP = PL::pstride(0);
+  constexpr int Nh = M / 3;
+  constexpr int NQ = S / 2 + 1;
+  static_assert(S % 2 == 0, "paired unpack needs an even stride");
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  C* __restrict__ w0 = static_cast<C*>(a.w0);
+  C* __restrict__ w1 = static_cast<C*>(a.w1);
+  for (int w = tid; w < V * NQ; w += NT) {
+    const int v = w % V;
+    const int q = w / V;
+    const bool two = q > 0 && 2 * q < S;
+    const int i2 = S - q;
+    C y1[R], y2[R];
+    {
+      const C* p = sm + PL::phys(q) * V + v;
+#pragma unroll
+      for (int k = 0; k < R; ++k) y1[k] = p[k * SP * V];
+      apply_tw<R, -1>(y1, tw + q * R);
+      Dft<R, -1, C>::run(y1);
+    }
+    if (two) {
+      const C* p = sm + PL::phys(i2) * V + v;
+#pragma unroll
+      for (int k = 0; k < R; ++k) y2[k] = p[k * SP * V];
+      apply_tw<R, -1>(y2, tw + i2 * R);
+      Dft<R, -1, C>::run(y2);
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) y2[k] = C{T(0), T(0)};
+    }
+    const size_t col = (size_t)z0 + v;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (j * S >= Nh) continue;  // folded at compile time
+      const int k1 = q + j * S;
+      if (j * S + S - 1 < Nh || k1 < Nh) {
+        const C p = y1[j];
+        const C c = (q == 0) ? y1[(R - j) % R] : (two ? y2[R - 1 - j] : y1[R - 1 - j]);
+        w0[(size_t)k1 * M + col] = C{T(0.5) * (p.x + c.x), T(0.5) * (p.y - c.y)};
+        w1[(size_t)k1 * M + col] = C{T(0.5) * (p.y + c.y), T(-0.5) * (p.x - c.x)};
+      }
+      const int k2 = i2 + j * S;
+      if (two && (j * S + S - 1 < Nh || k2 < Nh)) {
+        const C p = y2[j];
+        const C c = y1[R - 1 - j];
+        w0[(size_t)k2 * M + col] = C{T(0.5) * (p.x + c.x), T(0.5) * (p.y - c.y)};
+        w1[(size_t)k2 * M + col] = C{T(0.5) * (p.y + c.y), T(-0.5) * (p.x - c.x)};
+      }
+    }
+  }
 }
 
 // k_row: U-state rows -> P-state rows (products), optional CFL statistics.
@@ -225,9 +291,10 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a) {
     for (int w = tid; w < NB; w += NT) {
       const int v = w % V;
       const int b = w / V;
+      C* p = sm + b * (R + 1) * V + v;
       C x[R];
 #pragma unroll
-      for (int j = 0; j < R; ++j) x[j] = sm[PL::phys(b * R + j) * V + v];
+      for (int j = 0; j < R; ++j) x[j] = p[j * V];
       Dft<R, +1, C>::run(x);
       if (stats) {
 #pragma unroll
@@ -247,17 +314,19 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a) {
       }
       Dft<R, -1, C>::run(x);
 #pragma unroll
-      for (int j = 0; j < R; ++j) sm[PL::phys(b * R + j) * V + v] = x[j];
+      for (int j = 0; j < R; ++j) p[j * V] = x[j];
     }
     __syncthreads();
   }
-  dit_range<T, PL, V, NT, -1, PL::NP - 2, 0>(sm, tw, tid);
-
-  // unpack P = FFT(a + i b) into A = F(a), B = F(b) for kx < N/2 and store
-  {
+  if constexpr (sizeof(C) == 8) {
+    dit_range<T, PL, V, NT, -1, PL::NP - 2, 1>(sm, tw, tid);
+    row_last_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
+  } else {
+    dit_range<T, PL, V, NT, -1, PL::NP - 2, 0>(sm, tw, tid);
+    // unpack P = FFT(a + i b) into A = F(a), B = F(b) for kx < N/2 and store
     C* __restrict__ w0 = static_cast<C*>(a.w0);
     C* __restrict__ w1 = static_cast<C*>(a.w1);
-    const int Nh = a.N >> 1;
+    constexpr int Nh = M / 3;
     for (int w = tid; w < V * Nh; w += NT) {
       const int v = w % V;
       const int k = w / V;
@@ -322,7 +391,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
   constexpr int V = 2;
   const int tid = threadIdx.x;
   const int kx = blockIdx.x;
-  const int N = a.N, Nh = N >> 1;
+  constexpr int N = 2 * M / 3, Nh = M / 3;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   C* __restrict__ w0 = static_cast<C*>(a.w0);
   C* __restrict__ w1 = static_cast<C*>(a.w1);
@@ -366,51 +435,58 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
 #pragma unroll
       for (int j = 0; j < R; ++j) x[j] = src[i + j * S];
       Dft<R, -1, C>::run(x);
+      apply_tw<R, -1>(x, tw + i * R);
+      C* p = sm + PL::phys(i) * V + v;
 #pragma unroll
-      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<-1>(tw, i * k));
-#pragma unroll
-      for (int k = 0; k < R; ++k) sm[PL::phys(i + k * S) * V + v] = x[k];
+      for (int k = 0; k < R; ++k) p[k * PL::pstride(0) * V] = x[k];
     }
     __syncthreads();
   }
   dif_range<T, PL, V, NT, -1, 1, PL::NP - 1>(sm, tw, tid);
 
-  // middle: last forward DIF -> nonlinear term, update, inversion -> first inverse DIT
+  // middle: last forward DIF -> nonlinear term, update, inversion -> first inverse DIT.
+  // The two lanes of a butterfly hold A and B; lane 0 updates the even
+  // positions and lane 1 the odd ones, trading operands and results by shuffle.
+  // When 3 divides the radix, the de-aliased band (frequencies N/2 .. N-1, the
+  // middle third of the positions) is known at compile time and skipped.
   {
     constexpr int R = PL::RP;
     constexpr int NB = V * (M / R);
     constexpr int FSTEP = M / R;
+    constexpr bool BAND_CT = (R % 3 == 0) && ((R / 3) % 2 == 0);
     const T ax = T(kx);
     for (int w0i = 0; w0i < NB; w0i += NT) {
       const int w = w0i + tid;
       const bool act = w < NB;
       const int v = w & 1;
       const int b = act ? (w >> 1) : 0;
+      C* p = sm + b * (R + 1) * V + v;
       C x[R];
 #pragma unroll
-      for (int j = 0; j < R; ++j) x[j] = act ? sm[PL::phys(b * R + j) * V + v] : C{T(0), T(0)};
+      for (int j = 0; j < R; ++j) x[j] = act ? p[j * V] : C{T(0), T(0)};
       Dft<R, -1, C>::run(x);
       const int fb = PL::freq(b * R);
 #pragma unroll
-      for (int j = 0; j < R; ++j) {
-        const int f = fb + j * FSTEP;
-        const bool inband = act && (f < Nh || f >= N);
+      for (int j = 0; j < R; j += 2) {
+        if (BAND_CT && j >= R / 3 && j < 2 * R / 3) {
+          x[j] = C{T(0), T(0)};
+          x[j + 1] = C{T(0), T(0)};
+          continue;
+        }
+        // lane 0 takes position j, lane 1 position j+1
+        const C send = v == 0 ? x[j + 1] : x[j];
+        C recv;
+        recv.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
+        recv.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+        const C Az = v == 0 ? x[j] : recv;
+        const C Bz = v == 0 ? recv : x[j + 1];
+        const int f = fb + (j + v) * FSTEP;
+        const bool inband = act && (BAND_CT || f < Nh || f >= N);
         const int z = f < Nh ? f : f - Nh;
-        const C mine = x[j];
-        C oth;
-        oth.x = __shfl_xor_sync(0xffffffffu, mine.x, 1);
-        oth.y = __shfl_xor_sync(0xffffffffu, mine.y, 1);
-        C ld = {T(0), T(0)};
-        if (inband) ld = (v == 0) ? om[z] : fm[z];
-        C ldo;
-        ldo.x = __shfl_xor_sync(0xffffffffu, ld.x, 1);
-        ldo.y = __shfl_xor_sync(0xffffffffu, ld.y, 1);
-        C res = {T(0), T(0)};
+        C uh = {T(0), T(0)}, vh = {T(0), T(0)};
         if (inband) {
-          const C Az = v == 0 ? mine : oth;
-          const C Bz = v == 0 ? oth : mine;
-          const C o = v == 0 ? ld : ldo;
-          const C fo = v == 0 ? ldo : ld;
+          const C o = om[z];
+          const C fo = fm[z];
           const T gz = T(z < Nh ? z : z - N);
           const T K2 = ax * ax + gz * gz;
           const T GA = gz * ax;
@@ -425,26 +501,30 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
           C on;
           on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
           on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
-          if (v == 0) {
-            om[z] = on;
-          } else {
-            fm[z] = fn;
-          }
+          om[z] = on;
+          fm[z] = fn;
           if (kx >= 1) {
             const T ik = T(1) / K2;
             const C t = {on.x * ik, on.y * ik};
-            res = (v == 0) ? C{t.y * gz, -t.x * gz} : C{-t.y * ax, t.x * ax};
-          } else if (v == 0 && z >= 1) {
+            uh = C{t.y * gz, -t.x * gz};
+            vh = C{-t.y * ax, t.x * ax};
+          } else if (z >= 1) {
             const T ig = T(1) / gz;
-            res = C{on.y * ig, -on.x * ig};
+            uh = C{on.y * ig, -on.x * ig};
           }
         }
-        x[j] = res;
+        // lane 0 keeps u^ of position j and receives u^ of j+1; lane 1 the v^ pair
+        const C send2 = v == 0 ? vh : uh;
+        C recv2;
+        recv2.x = __shfl_xor_sync(0xffffffffu, send2.x, 1);
+        recv2.y = __shfl_xor_sync(0xffffffffu, send2.y, 1);
+        x[j] = v == 0 ? uh : recv2;
+        x[j + 1] = v == 0 ? recv2 : vh;
       }
       Dft<R, +1, C>::run(x);
       if (act) {
 #pragma unroll
-        for (int j = 0; j < R; ++j) sm[PL::phys(b * R + j) * V + v] = x[j];
+        for (int j = 0; j < R; ++j) p[j * V] = x[j];
       }
     }
     __syncthreads();
@@ -459,11 +539,11 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
       const int v = w & 1;
       const int i = w >> 1;
       C* __restrict__ dst = (v == 0 ? w0 : w1) + (size_t)kx * M;
+      const C* p = sm + PL::phys(i) * V + v;
       C x[R];
 #pragma unroll
-      for (int k = 0; k < R; ++k) x[k] = sm[PL::phys(i + k * S) * V + v];
-#pragma unroll
-      for (int k = 1; k < R; ++k) x[k] = cmul(x[k], twl<+1>(tw, i * k));
+      for (int k = 0; k < R; ++k) x[k] = p[k * PL::pstride(0) * V];
+      apply_tw<R, +1>(x, tw + i * R);
       Dft<R, +1, C>::run(x);
 #pragma unroll
       for (int j = 0; j < R; ++j) dst[i + j * S] = x[j];

@@ -1,65 +1,114 @@
-// Launch wrappers: one KernelSet per (precision, N), built from a radix plan,
-// a row-tile height V and the thread counts of the row and column kernels.
+// Launch wrappers and the autotuning candidates.
+//
+// For each (precision, N) the library compiles several row-pass and column-pass
+// candidates that differ in radix order (the Plan), rows per tile (V, row pass
+// only) and threads per block.  The two passes only share the data layout of
+// the work planes, so they are chosen independently; each carries its own
+// twiddle tables.  pal_create times every candidate on the handle's own state
+// and keeps the fastest (pal_autotune in pal_api.cu).
 #pragma once
 #include "pal_kernels.cuh"
 
 namespace pal {
 
-struct KernelSet {
-  int N, M, precision;
-  int V_row, NT_row, NT_col;
-  size_t smem_row, smem_col;
+struct RowKernels {
+  const char* name;
+  int V, NT;
+  size_t smem;
+  int tw_elems;
   cudaError_t (*configure)();
   void (*row)(const StepArgs&, cudaStream_t);
   void (*phys)(const StepArgs&, cudaStream_t);
+  void (*twiddles)(void* tw, cudaStream_t);
+};
+
+struct ColKernels {
+  const char* name;
+  int NT;
+  size_t smem;
+  int tw_elems;
+  cudaError_t (*configure)();
   void (*col)(const StepArgs&, cudaStream_t);
   void (*col_inv)(const StepArgs&, cudaStream_t);
+  void (*twiddles)(void* tw, cudaStream_t);
+};
+
+struct KernelSet {
+  int N, M, precision;
+  const RowKernels* rows;
+  int n_rows;
+  const ColKernels* cols;
+  int n_cols;
   void (*spectral)(const StepArgs&, cudaStream_t, int blocks);
   void (*transpose)(const void* in, void* out, int rows, int cols, int batch, cudaStream_t);
 };
 
 constexpr int kSpectralThreads = 256;
+constexpr size_t kSmemLimit = 227 * 1024;
 
-template <typename T, class PL, int VR, int NTR, int NTC>
-struct SetOf {
-  static constexpr int M = PL::M;
-  static constexpr size_t smem_row = size_t(PL::PADM) * VR * sizeof(cplx<T>);
-  static constexpr size_t smem_col = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
-  static_assert(smem_row <= 227 * 1024 && smem_col <= 227 * 1024, "tile does not fit in shared memory");
-  static_assert(M % VR == 0, "row tile must divide M");
+template <typename T, class PL>
+void launch_twiddles(void* tw, cudaStream_t s) {
+  k_twiddles<T, PL><<<(PL::TW_TOTAL + 255) / 256, 256, 0, s>>>(static_cast<cplx<T>*>(tw));
+}
 
+template <typename T, class PL, int V, int NT>
+struct RowOf {
+  static constexpr size_t smem = size_t(PL::PADM) * V * sizeof(cplx<T>);
+  static_assert(smem <= kSmemLimit, "row tile does not fit in shared memory");
+  static_assert(PL::M % V == 0, "row tile must divide M");
   static cudaError_t configure() {
-    cudaError_t e;
-    e = cudaFuncSetAttribute(k_row<T, PL, VR, NTR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
+    cudaError_t e = cudaFuncSetAttribute(k_row<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_phys<T, PL, VR, NTR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_col<T, PL, NTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_col_inv<T, PL, NTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
-  static void row(const StepArgs& a, cudaStream_t s) { k_row<T, PL, VR, NTR><<<M / VR, NTR, smem_row, s>>>(a); }
-  static void phys(const StepArgs& a, cudaStream_t s) { k_phys<T, PL, VR, NTR><<<M / VR, NTR, smem_row, s>>>(a); }
-  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NTC><<<a.N / 2, NTC, smem_col, s>>>(a); }
-  static void col_inv(const StepArgs& a, cudaStream_t s) { k_col_inv<T, PL, NTC><<<a.N / 2, NTC, smem_col, s>>>(a); }
-  static void spectral(const StepArgs& a, cudaStream_t s, int blocks) {
-    k_spectral<T, kSpectralThreads><<<blocks, kSpectralThreads, 0, s>>>(a);
-  }
-  static void transpose(const void* in, void* out, int rows, int cols, int batch, cudaStream_t s) {
-    dim3 grid((cols + 31) / 32, (rows + 31) / 32, batch);
-    k_transpose<T><<<grid, dim3(32, 8), 0, s>>>(static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), rows,
-                                                cols);
-  }
-  static const KernelSet* get(int N, int precision) {
-    static const KernelSet ks = {N,        M,          precision, VR,   NTR,     NTC,       smem_row,
-                                 smem_col, configure,  row,       phys, col,     col_inv,   spectral,
-                                 transpose};
-    return &ks;
+  static void row(const StepArgs& a, cudaStream_t s) { k_row<T, PL, V, NT><<<PL::M / V, NT, smem, s>>>(a); }
+  static void phys(const StepArgs& a, cudaStream_t s) { k_phys<T, PL, V, NT><<<PL::M / V, NT, smem, s>>>(a); }
+  static constexpr RowKernels make(const char* name) {
+    return RowKernels{name, V, NT, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
   }
 };
 
+template <typename T, class PL, int NT>
+struct ColOf {
+  static constexpr size_t smem = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
+  static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
+  static cudaError_t configure() {
+    cudaError_t e = cudaFuncSetAttribute(k_col<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT><<<a.N / 2, NT, smem, s>>>(a); }
+  static void col_inv(const StepArgs& a, cudaStream_t s) { k_col_inv<T, PL, NT><<<a.N / 2, NT, smem, s>>>(a); }
+  static constexpr ColKernels make(const char* name) {
+    return ColKernels{name, NT, smem, PL::TW_TOTAL, configure, col, col_inv, launch_twiddles<T, PL>};
+  }
+};
+
+template <typename T>
+void launch_spectral(const StepArgs& a, cudaStream_t s, int blocks) {
+  k_spectral<T, kSpectralThreads><<<blocks, kSpectralThreads, 0, s>>>(a);
+}
+
+template <typename T>
+void launch_transpose(const void* in, void* out, int rows, int cols, int batch, cudaStream_t s) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32, batch);
+  k_transpose<T><<<grid, dim3(32, 8), 0, s>>>(static_cast<const cplx<T>*>(in), static_cast<cplx<T>*>(out), rows,
+                                              cols);
+}
+
+#define PAL_KERNEL_SET(T, PREC, N, ROWS, COLS)                                                          \
+  static const ::pal::KernelSet kSet##N = {N,                                                           \
+                                           3 * (N) / 2,                                                 \
+                                           PREC,                                                        \
+                                           ROWS,                                                        \
+                                           (int)(sizeof(ROWS) / sizeof(ROWS[0])),                       \
+                                           COLS,                                                        \
+                                           (int)(sizeof(COLS) / sizeof(COLS[0])),                       \
+                                           ::pal::launch_spectral<T>,                                   \
+                                           ::pal::launch_transpose<T>};
+
 }  // namespace pal
 
-// Per-precision tables, defined in pal_inst_f32.cu / pal_inst_f64.cu.
+// Per-precision lookup (pal_inst_f32.cu / pal_inst_f64.cu); nullptr if unsupported.
 const pal::KernelSet* pal_kernels_f32(int N);
 const pal::KernelSet* pal_kernels_f64(int N);

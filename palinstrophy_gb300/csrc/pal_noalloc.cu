@@ -47,17 +47,9 @@ constexpr size_t kOffFields = kOffTwiddles + 16 * 1024;
 std::mutex g_setup_mutex;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// Scalars for this call (counters start at zero) and the FP32 twiddle table
-// exp(-2 pi i m / M) evaluated in double and rounded once.
-__global__ void k_noalloc_init(pal::DevScalars* sc, float2* tw, int M, double dt, double visc, double cn,
-                               double cnm1) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < M) {
-    double s, c;
-    sincospi(2.0 * (double)m / (double)M, &s, &c);
-    tw[m] = make_float2((float)c, (float)-s);
-  }
-  if (m == 0) {
+// Scalars for this call; the reduction counters must start at zero.
+__global__ void k_noalloc_init(pal::DevScalars* sc, double dt, double visc, double cn, double cnm1) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
     pal::DevScalars z = {};
     z.dt = dt;
     z.cn = cn;
@@ -100,37 +92,50 @@ extern "C" int pal_step_noalloc(int N, int method, int nsteps, double dt, double
   pal::StepArgs a = {};
   a.sc = reinterpret_cast<pal::DevScalars*>(base + kOffScalars);
   a.part = reinterpret_cast<double*>(base + kOffPartials);
-  a.tw = base + kOffTwiddles;
+  a.tw = base + kOffTwiddles;  // row-pass table; the column table follows at +8 KB
   a.om = base + kOffFields;
   a.fnm1 = base + kOffFields + plane_om;
   a.w0 = base + kOffFields + 2 * plane_om;
   a.w1 = base + kOffFields + 2 * plane_om + plane_w;
   a.N = N;
 
-  k_noalloc_init<<<(M + 255) / 256, 256, 0, s>>>(a.sc, static_cast<float2*>(const_cast<void*>(a.tw)), M, dt, visc,
-                                                  cn, cnm1);
+  const pal::RowKernels& rk = ks->rows[0];
+  const pal::ColKernels& ck = ks->cols[0];
+  const size_t tw_half = (kOffFields - kOffTwiddles) / 2;
+  if ((size_t)rk.tw_elems * sizeof(float2) > tw_half || (size_t)ck.tw_elems * sizeof(float2) > tw_half)
+    return PAL_ERR_INVALID;
+  void* tw_row = base + kOffTwiddles;
+  void* tw_col = base + kOffTwiddles + tw_half;
+  k_noalloc_init<<<1, 32, 0, s>>>(a.sc, dt, visc, cn, cnm1);
+  rk.twiddles(tw_row, s);
+  ck.twiddles(tw_col, s);
   ks->transpose(om2, a.om, N, Nh, 1, s);      // caller layout (N, N/2) -> [kx][z]
   ks->transpose(fnm1, a.fnm1, N, Nh, 1, s);
   a.src = nullptr;                             // velocity from the om2 inversion
-  ks->col_inv(a, s);
+  a.tw = tw_col;
+  ck.col_inv(a, s);
   for (int j = 0; j < nsteps; ++j) {
     if (method == PAL_CNAB2) {
       a.flags = 0;
-      ks->row(a, s);
+      a.tw = tw_row;
+      rk.row(a, s);
       a.flags = pal::F_CNM1 | pal::F_ADVANCE;
       a.scheme = 0;
-      ks->col(a, s);
+      a.tw = tw_col;
+      ck.col(a, s);
     } else {
       static const double alpha[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
       static const double beta[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0};
       for (int st = 0; st < 3; ++st) {
         a.flags = 0;
-        ks->row(a, s);
+        a.tw = tw_row;
+        rk.row(a, s);
         a.flags = st == 2 ? pal::F_ADVANCE : 0;
         a.scheme = 1;
         a.alpha = alpha[st];
         a.beta = beta[st];
-        ks->col(a, s);
+        a.tw = tw_col;
+        ck.col(a, s);
       }
     }
   }

@@ -159,6 +159,18 @@ class Field:
                                               L.ctypes.byref(c), L.ctypes.byref(n)))
         return r.value, c.value, n.value
 
+    def variant(self) -> dict:
+        """The kernel candidates the autotuner selected for this size."""
+        r, c, nr, nc = L._I(), L._I(), L._I(), L._I()
+        buf = L.ctypes.create_string_buffer(256)
+        self._ck(self.lib.pal_get_variant(self.h, L.ctypes.byref(r), L.ctypes.byref(c), L.ctypes.byref(nr),
+                                          L.ctypes.byref(nc), buf, len(buf)))
+        return {"row": r.value, "col": c.value, "n_rows": nr.value, "n_cols": nc.value,
+                "desc": buf.value.decode()}
+
+    def set_variant(self, row: int, col: int):
+        self._ck(self.lib.pal_set_variant(self.h, int(row), int(col)))
+
     def stream_ptr(self) -> int:
         p = L._P()
         self._ck(self.lib.pal_get_stream(self.h, L.ctypes.byref(p)))

@@ -292,3 +292,39 @@ def test_dropin_run_dns(ts, capsys):
     assert S.it == 21
     U, Lh, tau = S.flow_eddy_metrics()
     assert U > 0 and Lh > 0 and tau > 0
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
+@pytest.mark.parametrize("N", [256, 512, 1024, 4096])
+def test_every_kernel_candidate_agrees(ts, prec, tol, N):
+    """Each compiled row/column candidate (radix order, tile height, threads)
+    gives the same field, so the autotuner's choice never changes results
+    beyond rounding; at N <= 1024 the default candidates also match the oracle."""
+    from palinstrophy_gb300 import _lib as L
+    om2, uc, st = L.pao_generate(N, 12.0, 1e4, 7, "KM3")
+    F = ts.Field(N, prec, 1e4, 0.3)
+    v = F.variant()
+    assert v["desc"].startswith("row[")
+    F.set_state(om2, None, uc)
+    F.step2a()
+    dt = 0.3 / (F.compute_cflm() * math.pi)  # a stable step (CFL 0.3) at every N
+    results = {}
+    for r, c in [(r, 0) for r in range(v["n_rows"])] + [(0, c) for c in range(1, v["n_cols"])]:
+        F.set_variant(r, c)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.set_scalar("dt", dt)
+        F.set_scalar("cnm1", 0.0)
+        F.step("LS_IMEX_RK3", 2, update=0)
+        results[(r, c)] = F.om2().astype(np.complex128)
+    ref = results[(0, 0)]
+    for key, om in results.items():
+        assert do.rel_l2(ref, om) <= tol, key
+    if N <= 1024:
+        S = do.OracleState(N, om2, uc, st["visc"], 0.3)
+        do.step2a(S)
+        S.dt = dt
+        for _ in range(2):
+            do.rk3(S)
+        assert do.rel_l2(S.om2, ref) <= tol
+    F.close()

@@ -35,6 +35,7 @@ def env(built_lib):
 
 def _reference_path(Field, om2, fnm1, method, nsteps, dt, visc, cn, cnm1):
     F = Field(om2.shape[0], "fp32", 1e4, 0.5)
+    F.set_variant(0, 0)  # the kernel candidates pal_step_noalloc runs
     F.set_state(om2, fnm1, None)
     for k, v in (("dt", dt), ("visc", visc), ("cn", cn), ("cnm1", cnm1)):
         F.set_scalar(k, v)
@@ -51,7 +52,7 @@ def test_two_calls_match_allocating_path(env, method, code):
     N = 256
     om2 = d["om2"].astype(np.complex64)
     fnm1 = np.zeros_like(om2)
-    visc, dt = float(d["visc"]), 2e-3
+    visc, dt = float(d["visc"]), 1e-3  # CFL about 0.5 at this N
     lib = L.load()
     dom = torch.from_numpy(om2.copy()).cuda()
     dfn = torch.from_numpy(fnm1.copy()).cuda()

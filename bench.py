@@ -354,10 +354,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
                     help="profiling target: init + 2 warm-up + 2 timed steps of one precision, no JSON")
+    ap.add_argument("--variant", default=None,
+                    help="row,col kernel candidates for --ncu-case (skips the autotuning launches)")
     args = ap.parse_args()
     if args.ncu_case:
+        if args.variant:
+            os.environ["PAL_AUTOTUNE"] = "0"
         om2, uc, st = _init_arrays()
         F = _field(args.ncu_case, om2, uc, st["visc"])
+        if args.variant:
+            r, c = (int(x) for x in args.variant.split(","))
+            F.set_variant(r, c)
         F.step(METHOD, 2)
         F.step(METHOD, 2)
         F.synchronize()

@@ -191,6 +191,7 @@ struct Plan {
     return o;
   }
   static constexpr int TW_TOTAL = tw_off(NP);
+  static constexpr int TW_MODE = 0;  // full [i][k] tables
   // frequency index of the DIF output stored at position pos (every constant
   // is a template-time value, so no radix table is touched at run time)
   template <int Q>
@@ -209,6 +210,20 @@ struct Plan {
     freq_digits<0>(pos, f);
     return f;
   }
+};
+
+// The same plan with compact twiddle tables: per pass and butterfly only
+// (W^i, W^4i); the other powers are formed in registers (at most two products
+// of powers of the loaded values), trading load instructions for FMAs.
+template <class PL>
+struct Rec : PL {
+  static constexpr int TW_MODE = 1;
+  static constexpr int tw_off(int p) {
+    int o = 0;
+    for (int q = 0; q < p; ++q) o += 2 * PL::stride(q);
+    return o;
+  }
+  static constexpr int TW_TOTAL = tw_off(PL::NP);
 };
 
 // x * W^(SIGN) where w = exp(-2 pi i e / L) is a forward-table entry.
@@ -250,6 +265,50 @@ __device__ __forceinline__ void apply_tw(C (&x)[R], const C* __restrict__ t) {
   }
 }
 
+// Twiddles W^(k i), k = 1..R-1, from w1 = W^i and w4 = W^(4i): k = 4a + b,
+// W^(ki) = (W^(4i))^a * (W^i)^b with the powers built by repeated products.
+template <int R, int SIGN, typename C>
+__device__ __forceinline__ void apply_tw_rec(C (&x)[R], C w1, C w4) {
+  using T = decltype(w1.x);
+  C pb[4];
+  pb[0] = C{T(1), T(0)};
+  pb[1] = w1;
+  pb[2] = cmul(w1, w1);
+  pb[3] = cmul(pb[2], w1);
+  constexpr int NA = (R + 3) / 4;
+  C pa[NA > 1 ? NA : 2];
+  pa[0] = C{T(1), T(0)};
+  pa[1] = w4;
+#pragma unroll
+  for (int a = 2; a < NA; ++a) pa[a] = (a % 2 == 0) ? cmul(pa[a / 2], pa[a / 2]) : cmul(pa[a - 1], w4);
+#pragma unroll
+  for (int k = 1; k < R; ++k) {
+    const int a = k / 4, b = k % 4;
+    const C t = (a == 0) ? pb[b] : (b == 0 ? pa[a] : cmul(pa[a], pb[b]));
+    x[k] = twmul<SIGN>(x[k], t);
+  }
+}
+
+// Twiddles of butterfly i of pass P, in the plan's table mode.
+template <class PL, int P, int SIGN, int R, typename C>
+__device__ __forceinline__ void pass_tw(C (&x)[R], const C* __restrict__ tw, int i) {
+  if constexpr (PL::TW_MODE == 0) {
+    apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
+  } else {
+    const C* t = tw + PL::tw_off(P) + 2 * i;
+    C w1, w4;
+    if constexpr (sizeof(C) == 8) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(t));
+      w1 = C{v.x, v.y};
+      w4 = C{v.z, v.w};
+    } else {
+      w1 = __ldg(t);
+      w4 = __ldg(t + 1);
+    }
+    apply_tw_rec<R, SIGN>(x, w1, w4);
+  }
+}
+
 // One DIF pass p over a [slot][v] tile in shared memory.
 template <typename T, class PL, int V, int NT, int P, int SIGN>
 __device__ __forceinline__ void dif_pass(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
@@ -269,7 +328,7 @@ __device__ __forceinline__ void dif_pass(cplx<T>* sm, const cplx<T>* __restrict_
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = p[j * SP * V];
     Dft<R, SIGN, C>::run(x);
-    if constexpr (S > 1) apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
+    if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
 #pragma unroll
     for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
   }
@@ -293,7 +352,7 @@ __device__ __forceinline__ void dit_pass(cplx<T>* sm, const cplx<T>* __restrict_
     C x[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) x[k] = p[k * SP * V];
-    if constexpr (S > 1) apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
+    if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
     Dft<R, SIGN, C>::run(x);
 #pragma unroll
     for (int j = 0; j < R; ++j) p[j * SP * V] = x[j];
@@ -308,9 +367,11 @@ __device__ __forceinline__ double tw_angle(int e) {
     constexpr int R = PL::R[Q];
     constexpr int S = PL::stride(Q);
     constexpr int step = PL::M / PL::span(Q);
-    if (e < off + S * R) {
-      const int i = (e - off) / R;
-      const int k = (e - off) - i * R;
+    constexpr int W = PL::TW_MODE == 0 ? R : 2;  // entries per butterfly
+    if (e < off + S * W) {
+      const int i = (e - off) / W;
+      const int c = (e - off) - i * W;
+      const int k = PL::TW_MODE == 0 ? c : (c == 0 ? 1 : 4);
       return 2.0 * (double)((long long)step * i * k) / (double)PL::M;
     }
     return tw_angle<PL, Q + 1>(e);

@@ -196,7 +196,7 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
       x[j] = zz;
     }
     Dft<R, +1, C>::run(x);
-    apply_tw<R, +1>(x, tw + i * R);
+    pass_tw<PL, 0, +1>(x, tw, i);
     C* p = sm + PL::phys(i) * V + v;
 #pragma unroll
     for (int k = 0; k < R; ++k) p[k * PL::pstride(0) * V] = x[k];
@@ -233,14 +233,14 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
       const C* p = sm + PL::phys(q) * V + v;
 #pragma unroll
       for (int k = 0; k < R; ++k) y1[k] = p[k * SP * V];
-      apply_tw<R, -1>(y1, tw + q * R);
+      pass_tw<PL, 0, -1>(y1, tw, q);
       Dft<R, -1, C>::run(y1);
     }
     if (two) {
       const C* p = sm + PL::phys(i2) * V + v;
 #pragma unroll
       for (int k = 0; k < R; ++k) y2[k] = p[k * SP * V];
-      apply_tw<R, -1>(y2, tw + i2 * R);
+      pass_tw<PL, 0, -1>(y2, tw, i2);
       Dft<R, -1, C>::run(y2);
     } else {
 #pragma unroll
@@ -381,8 +381,18 @@ struct ModeCoef {
   T h1, h2, c2, c3, divxz;
 };
 
-// k_col: P-state column -> (om, fnm1 update) -> U-state column.
-template <typename T, class PL, int NT>
+// 16-byte asynchronous global -> shared copies (Ampere+ cp.async).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF the
+// column's om and fnm1 are copied into shared memory asynchronously at entry,
+// so the update reads them without exposed global latency.
+template <typename T, class PL, int NT, bool PREF>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -397,6 +407,18 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
   C* __restrict__ w1 = static_cast<C*>(a.w1);
   C* __restrict__ om = static_cast<C*>(a.om) + (size_t)kx * N;
   C* __restrict__ fm = static_cast<C*>(a.fnm1) + (size_t)kx * N;
+  C* s_om = sm + PL::PADM * V;
+  C* s_fm = s_om + N;
+  if constexpr (PREF) {
+    constexpr int CH = N * (int)sizeof(C) / 16;
+    for (int c = tid; c < 2 * CH; c += NT) {
+      const bool second = c >= CH;
+      const int cc = second ? c - CH : c;
+      cp_async16(reinterpret_cast<char*>(second ? s_fm : s_om) + 16 * cc,
+                 reinterpret_cast<const char*>(second ? fm : om) + 16 * cc);
+    }
+    cp_async_commit();
+  }
 
   // implicit / explicit weights, formed in FP64 from the device scalars
   ModeCoef<T> cf;
@@ -435,7 +457,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
 #pragma unroll
       for (int j = 0; j < R; ++j) x[j] = src[i + j * S];
       Dft<R, -1, C>::run(x);
-      apply_tw<R, -1>(x, tw + i * R);
+      pass_tw<PL, 0, -1>(x, tw, i);
       C* p = sm + PL::phys(i) * V + v;
 #pragma unroll
       for (int k = 0; k < R; ++k) p[k * PL::pstride(0) * V] = x[k];
@@ -443,6 +465,10 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
     __syncthreads();
   }
   dif_range<T, PL, V, NT, -1, 1, PL::NP - 1>(sm, tw, tid);
+  if constexpr (PREF) {
+    cp_async_wait_all();
+    __syncthreads();
+  }
 
   // middle: last forward DIF -> nonlinear term, update, inversion -> first inverse DIT.
   // The two lanes of a butterfly hold A and B; lane 0 updates the even
@@ -485,8 +511,8 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
         const int z = f < Nh ? f : f - Nh;
         C uh = {T(0), T(0)}, vh = {T(0), T(0)};
         if (inband) {
-          const C o = om[z];
-          const C fo = fm[z];
+          const C o = PREF ? s_om[z] : om[z];
+          const C fo = PREF ? s_fm[z] : fm[z];
           const T gz = T(z < Nh ? z : z - N);
           const T K2 = ax * ax + gz * gz;
           const T GA = gz * ax;
@@ -543,7 +569,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
       C x[R];
 #pragma unroll
       for (int k = 0; k < R; ++k) x[k] = p[k * PL::pstride(0) * V];
-      apply_tw<R, +1>(x, tw + i * R);
+      pass_tw<PL, 0, +1>(x, tw, i);
       Dft<R, +1, C>::run(x);
 #pragma unroll
       for (int j = 0; j < R; ++j) dst[i + j * S] = x[j];

@@ -68,17 +68,21 @@ struct RowOf {
   }
 };
 
-template <typename T, class PL, int NT>
+template <typename T, class PL, int NT, bool PREF = false>
 struct ColOf {
-  static constexpr size_t smem = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
+  static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
+  static constexpr size_t smem = smem_inv + (PREF ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
   static cudaError_t configure() {
-    cudaError_t e = cudaFuncSetAttribute(k_col<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_col<T, PL, NT, PREF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
-  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT><<<a.N / 2, NT, smem, s>>>(a); }
-  static void col_inv(const StepArgs& a, cudaStream_t s) { k_col_inv<T, PL, NT><<<a.N / 2, NT, smem, s>>>(a); }
+  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF><<<a.N / 2, NT, smem, s>>>(a); }
+  static void col_inv(const StepArgs& a, cudaStream_t s) {
+    k_col_inv<T, PL, NT><<<a.N / 2, NT, smem_inv, s>>>(a);
+  }
   static constexpr ColKernels make(const char* name) {
     return ColKernels{name, NT, smem, PL::TW_TOTAL, configure, col, col_inv, launch_twiddles<T, PL>};
   }

@@ -159,6 +159,34 @@ int pal_last_error(pal_handle* h, char* buf, size_t n);
 int pal_step_noalloc(int N, int method, int nsteps, double dt, double visc, double cn, double cnm1,
                      void* om2, void* fnm1, void* stream);
 
+/* Batched ensembles (the reference runs one field per process; this is the
+ * GB300 form for many independent fields): members with their own N, seed,
+ * viscosity, CFL target and adaptive dt advance together, one launch per
+ * group of equal N per pass (grid.y = members), optionally replayed from a
+ * CUDA graph.  No counterpart in the reference API; each member follows the
+ * single-field semantics of pal_step. */
+typedef struct pal_ensemble pal_ensemble;
+int pal_ensemble_create(int n_members, const int* N, int precision, double Re, double cfl, pal_ensemble** out);
+int pal_ensemble_destroy(pal_ensemble* e);
+/* Member state in the reference layouts (as pal_set_spectral_state +
+ * pal_set_velocity_spectrum); fnm1 / uc_low may be NULL. */
+int pal_ensemble_set_member(pal_ensemble* e, int member, const void* om2, const void* fnm1, const void* uc_low);
+/* One scalar (PAL_SC_*) of one member, or of all members with member = -1. */
+int pal_ensemble_set_scalar(pal_ensemble* e, int member, int which, double value);
+/* Initial STEP2A + CFLM + dt = cflnum/(CFLM pi), cn = 1, cnm1 = 0 per member
+ * (turbo_simulator.py:2810-2823), on the device. */
+int pal_ensemble_init_dt(pal_ensemble* e);
+/* nsteps steps of every member with NEXTDT per member after iterations
+ * it % update == 0 or it == 1 (update > 0); use_graph captures the launch
+ * sequence once per pattern and replays it. */
+int pal_ensemble_step(pal_ensemble* e, int method, int nsteps, int update, int use_graph);
+int pal_ensemble_get_member(pal_ensemble* e, int member, int which, void* host_dst);
+int pal_ensemble_get_scalars(pal_ensemble* e, int member, double* t, double* dt, double* cn, double* cflm,
+                             long long* it);
+int pal_ensemble_get_stream(pal_ensemble* e, void** stream);
+int pal_ensemble_synchronize(pal_ensemble* e);
+int pal_ensemble_last_error(pal_ensemble* e, char* buf, size_t n);
+
 /* Host-side PAO / KM3 initial condition (turbo_simulator.py:213-485, 1059-1239,
  * 1314-1361), complex64 outputs: om2 (N, N/2) and uc_low (2, N, N/2).
  * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed. */

@@ -74,6 +74,17 @@ _SIGS = {
     "pal_set_variant": (_I, [_H, _I, _I]),
     "pal_profile_kernels": (_I, [_H, _I, _I, _DP, _DP, ctypes.POINTER(_I)]),
     "pal_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
+    "pal_ensemble_create": (_I, [_I, ctypes.POINTER(_I), _I, _D, _D, ctypes.POINTER(_H)]),
+    "pal_ensemble_destroy": (_I, [_H]),
+    "pal_ensemble_set_member": (_I, [_H, _I, _P, _P, _P]),
+    "pal_ensemble_set_scalar": (_I, [_H, _I, _I, _D]),
+    "pal_ensemble_init_dt": (_I, [_H]),
+    "pal_ensemble_step": (_I, [_H, _I, _I, _I, _I]),
+    "pal_ensemble_get_member": (_I, [_H, _I, _I, _P]),
+    "pal_ensemble_get_scalars": (_I, [_H, _I, _DP, _DP, _DP, _DP, ctypes.POINTER(ctypes.c_longlong)]),
+    "pal_ensemble_get_stream": (_I, [_H, ctypes.POINTER(_P)]),
+    "pal_ensemble_synchronize": (_I, [_H]),
+    "pal_ensemble_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
     "pal_step_noalloc": (_I, [_I, _I, _I, _D, _D, _D, _D, _P, _P, _P]),
     "pal_pao_generate": (_I, [_I, _D, _D, _I, _I, _P, _P, _DP, ctypes.POINTER(_I)]),
 }

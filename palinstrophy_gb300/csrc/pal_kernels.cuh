@@ -58,7 +58,27 @@ struct StepArgs {
   double c2, c3;    // explicit weights of fn and fnm1
   double alpha, beta;
   int scheme;       // 0 = CNAB2 (coefficients from device dt/cnm1), 1 = RK3 stage
+  // Batched ensembles: blockIdx.y selects the member; every per-member array
+  // advances by its stride (in elements) and sc by one DevScalars per member.
+  int members;      // grid.y of the launch (>= 1)
+  long long ms_w, ms_om, ms_part, ms_phys, ms_src;
 };
+
+// Member view of the arguments for block row blockIdx.y.
+__device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz) {
+  const long long m = blockIdx.y;
+  if (m == 0) return a;
+  StepArgs b = a;
+  b.w0 = static_cast<char*>(a.w0) + m * a.ms_w * esz;
+  b.w1 = static_cast<char*>(a.w1) + m * a.ms_w * esz;
+  b.om = static_cast<char*>(a.om) + m * a.ms_om * esz;
+  b.fnm1 = static_cast<char*>(a.fnm1) + m * a.ms_om * esz;
+  if (a.phys) b.phys = static_cast<char*>(a.phys) + m * a.ms_phys * (esz / 2);
+  if (a.src) b.src = static_cast<const char*>(a.src) + m * a.ms_src * esz;
+  b.sc = a.sc + m;
+  b.part = a.part + m * a.ms_part;
+  return b;
+}
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -113,7 +133,7 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
   __syncthreads();
   if (tid == 0) {
     const unsigned int ticket = atomicAdd(counter, 1u);
-    is_last = (ticket == gridDim.x * gridDim.y - 1u);
+    is_last = (ticket == gridDim.x - 1u);  // blocks of this member (grid row)
   }
   __syncthreads();
   return is_last != 0;
@@ -128,12 +148,12 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, int M, in
   double s1[1] = {sum};
   block_sum<NT, 1>(s1, red, tid);
   if (tid == 0) {
-    a.part[2 * (blockIdx.x + gridDim.x * blockIdx.y)] = mx;
-    a.part[2 * (blockIdx.x + gridDim.x * blockIdx.y) + 1] = s1[0];
+    a.part[2 * blockIdx.x] = mx;
+    a.part[2 * blockIdx.x + 1] = s1[0];
   }
   const bool last = last_block(&a.sc->row_counter, tid);
   if (!last) return;
-  const int nb = gridDim.x * gridDim.y;
+  const int nb = gridDim.x;
   double m2 = 0.0, s2[1] = {0.0};
   for (int q = tid; q < nb; q += NT) {
     m2 = fmax(m2, __ldcg(a.part + 2 * q));
@@ -270,8 +290,9 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
 
 // k_row: U-state rows -> P-state rows (products), optional CFL statistics.
 template <typename T, class PL, int V, int NT>
-__global__ void __launch_bounds__(NT) k_row(StepArgs a) {
+__global__ void __launch_bounds__(NT) k_row(StepArgs a0) {
   using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
@@ -341,8 +362,9 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a) {
 
 // k_phys: U-state rows -> physical u, v (statistics, optional plane store).
 template <typename T, class PL, int V, int NT>
-__global__ void __launch_bounds__(NT) k_phys(StepArgs a) {
+__global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
   using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
@@ -393,8 +415,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // column's om and fnm1 are copied into shared memory asynchronously at entry,
 // so the update reads them without exposed global latency.
 template <typename T, class PL, int NT, bool PREF>
-__global__ void __launch_bounds__(NT) k_col(StepArgs a) {
+__global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
@@ -593,8 +616,9 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a) {
 // uc_full) or, when src is null, from the omega -> velocity inversion of om
 // (turbo_simulator.py:1555-1585).
 template <typename T, class PL, int NT>
-__global__ void __launch_bounds__(NT) k_col_inv(StepArgs a) {
+__global__ void __launch_bounds__(NT) k_col_inv(StepArgs a0) {
   using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
@@ -647,8 +671,9 @@ __global__ void __launch_bounds__(NT) k_col_inv(StepArgs a) {
 // rfft weights w = [1, 2, ..., 2, 1] of turbo_simulator.py:778-781 and
 // turbo_main.py:2040-2044.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_spectral(StepArgs a) {
+__global__ void __launch_bounds__(NT) k_spectral(StepArgs a0) {
   using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
   const C* __restrict__ om = static_cast<const C*>(a.om);
   const int N = a.N, Nh = N >> 1;
   const long long total = (long long)N * Nh;

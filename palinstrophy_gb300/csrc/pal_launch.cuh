@@ -61,8 +61,12 @@ struct RowOf {
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
-  static void row(const StepArgs& a, cudaStream_t s) { k_row<T, PL, V, NT><<<PL::M / V, NT, smem, s>>>(a); }
-  static void phys(const StepArgs& a, cudaStream_t s) { k_phys<T, PL, V, NT><<<PL::M / V, NT, smem, s>>>(a); }
+  static void row(const StepArgs& a, cudaStream_t s) {
+    k_row<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
+  }
+  static void phys(const StepArgs& a, cudaStream_t s) {
+    k_phys<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
+  }
   static constexpr RowKernels make(const char* name) {
     return RowKernels{name, V, NT, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
   }
@@ -79,9 +83,11 @@ struct ColOf {
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
-  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF><<<a.N / 2, NT, smem, s>>>(a); }
+  static void col(const StepArgs& a, cudaStream_t s) {
+    k_col<T, PL, NT, PREF><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
+  }
   static void col_inv(const StepArgs& a, cudaStream_t s) {
-    k_col_inv<T, PL, NT><<<a.N / 2, NT, smem_inv, s>>>(a);
+    k_col_inv<T, PL, NT><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem_inv, s>>>(a);
   }
   static constexpr ColKernels make(const char* name) {
     return ColKernels{name, NT, smem, PL::TW_TOTAL, configure, col, col_inv, launch_twiddles<T, PL>};
@@ -90,7 +96,7 @@ struct ColOf {
 
 template <typename T>
 void launch_spectral(const StepArgs& a, cudaStream_t s, int blocks) {
-  k_spectral<T, kSpectralThreads><<<blocks, kSpectralThreads, 0, s>>>(a);
+  k_spectral<T, kSpectralThreads><<<dim3(blocks, a.members > 1 ? a.members : 1), kSpectralThreads, 0, s>>>(a);
 }
 
 template <typename T>

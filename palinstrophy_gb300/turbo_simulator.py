@@ -433,3 +433,82 @@ def main():
 
 if __name__ == "__main__":
     main()
+
+
+class Ensemble:
+    """Many independent fields (members) of possibly different N, stepped together.
+
+    Each member keeps its own viscosity, CFL target and adaptive dt.  One kernel
+    launch per group of equal N per pass; with ``graph=True`` the launch
+    sequence of a step call is captured once as a CUDA graph and replayed.
+    """
+
+    def __init__(self, Ns, precision="fp32", Re=1e4, cfl=0.5):
+        self.lib = L.load()
+        self.Ns = [int(n) for n in Ns]
+        self.precision = precision
+        self.cdt = np.complex64 if precision == "fp32" else np.complex128
+        arr = (L._I * len(self.Ns))(*self.Ns)
+        h = L._H()
+        rc = self.lib.pal_ensemble_create(len(self.Ns), arr, _PREC[precision], float(Re), float(cfl), h)
+        if rc != L.PAL_OK:
+            raise L.PalError(rc, self._err(None))
+        self.h = h
+
+    def _err(self, h):
+        buf = L.ctypes.create_string_buffer(512)
+        self.lib.pal_ensemble_last_error(h, buf, len(buf))
+        return buf.value.decode()
+
+    def _ck(self, rc):
+        if rc != L.PAL_OK:
+            raise (ValueError(self._err(self.h)) if rc == L.PAL_ERR_INVALID else L.PalError(rc, self._err(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pal_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_member(self, m, om2, fnm1=None, uc_low=None):
+        om2 = np.ascontiguousarray(om2, dtype=self.cdt)
+        f = None if fnm1 is None else np.ascontiguousarray(fnm1, dtype=self.cdt)
+        u = None if uc_low is None else np.ascontiguousarray(uc_low, dtype=self.cdt)
+        self._ck(self.lib.pal_ensemble_set_member(self.h, int(m), L.ptr(om2), None if f is None else L.ptr(f),
+                                                  None if u is None else L.ptr(u)))
+
+    def set_scalar(self, m, which, value):
+        idx = {"t": L.PAL_SC_T, "dt": L.PAL_SC_DT, "cn": L.PAL_SC_CN, "cnm1": L.PAL_SC_CNM1,
+               "visc": L.PAL_SC_VISC, "cflnum": L.PAL_SC_CFLNUM}[which]
+        self._ck(self.lib.pal_ensemble_set_scalar(self.h, int(m), idx, float(value)))
+
+    def init_dt(self):
+        self._ck(self.lib.pal_ensemble_init_dt(self.h))
+
+    def step(self, method="CNAB2", nsteps=1, update=1, graph=True):
+        self._ck(self.lib.pal_ensemble_step(self.h, _METHODS[method], int(nsteps), int(update), int(bool(graph))))
+
+    def om2(self, m):
+        a = np.empty((self.Ns[m], self.Ns[m] // 2), self.cdt)
+        self._ck(self.lib.pal_ensemble_get_member(self.h, int(m), L.PAL_FIELD_OM2, L.ptr(a)))
+        return a
+
+    def scalars(self, m):
+        v = [L._D() for _ in range(4)]
+        it = L.ctypes.c_longlong()
+        self._ck(self.lib.pal_ensemble_get_scalars(self.h, int(m), *[L.ctypes.byref(x) for x in v],
+                                                   L.ctypes.byref(it)))
+        return dict(zip(("t", "dt", "cn", "cflm"), [x.value for x in v]), it=it.value)
+
+    def stream_ptr(self):
+        p = L._P()
+        self._ck(self.lib.pal_ensemble_get_stream(self.h, L.ctypes.byref(p)))
+        return p.value
+
+    def synchronize(self):
+        self._ck(self.lib.pal_ensemble_synchronize(self.h))

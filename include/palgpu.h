@@ -43,6 +43,7 @@ enum { PAL_FP32 = 0, PAL_FP64 = 1 };
 enum { PAL_CNAB2 = 0, PAL_LS_IMEX_RK3 = 1 };
 enum { PAL_FIELD_OM2 = 0, PAL_FIELD_FNM1 = 1, PAL_FIELD_UR_U = 2, PAL_FIELD_UR_V = 3 };
 enum { PAL_SPEC_KM3 = 0, PAL_SPEC_PAO = 1 };
+enum { PAL_VAR_U = 0, PAL_VAR_V = 1, PAL_VAR_ENERGY = 2, PAL_VAR_OMEGA = 3, PAL_VAR_STREAM = 4 };
 enum { PAL_SC_T = 0, PAL_SC_DT = 1, PAL_SC_CN = 2, PAL_SC_CNM1 = 3, PAL_SC_VISC = 4, PAL_SC_CFLNUM = 5, PAL_SC_IT = 6 };
 
 typedef struct pal_handle pal_handle;
@@ -115,6 +116,20 @@ int pal_compute_cflm(pal_handle* h, double* cflm);
 int pal_next_dt(pal_handle* h, int sync_host, double* cflm);
 /* flow_eddy_metrics + the GUI sums in one pass; waits. */
 int pal_diagnostics(pal_handle* h, pal_diag* out);
+
+/* Shell-binned kinetic-energy spectrum from om2 (compute_energy_spectrum_uv_bins,
+ * turbo_simulator.py:2225-2383): nbins bins of r = |k|/k_nyq over [0, r_max),
+ * esum[b] = sum |om|^2/K2 * (M^2)^2 (x2 for kx > 0), count[b] = modes (x2 for
+ * kx > 0); deterministic; waits. */
+int pal_energy_spectrum(pal_handle* h, int nbins, double r_max, double k_nyq, double* esum, int* count);
+
+/* Display fields of DnsSimulator (turbo_wrapper.py:353-413, turbo_simulator.py:
+ * 2629-2709) on the 3/2 grid, M x M: u, v, |u| (dns_kinetic), omega
+ * (dns_om2_phys) or the streamfunction (dns_stream_func), into host_field
+ * (real, handle precision) and/or host_pixels (uint8, normalised to 1..255,
+ * 128 if constant, as _float_to_pixels_gpu).  Uses separate scratch planes,
+ * so the simulation state is unchanged.  Waits. */
+int pal_vis_field(pal_handle* h, int var, void* host_field, unsigned char* host_pixels);
 
 /* Copy a field to host memory in the reference layout (waits). */
 int pal_get_field(pal_handle* h, int which, void* host_dst);

@@ -320,3 +320,39 @@ def rel_l2(ref, cand) -> float:
     ref = np.asarray(ref).astype(np.complex128)
     cand = np.asarray(cand).astype(np.complex128)
     return float(np.linalg.norm((cand - ref).ravel()) / max(np.linalg.norm(ref.ravel()), 1e-300))
+
+
+# ---------------- display fields (turbo_simulator.py:2629-2708) -------------
+def band_to_phys(S: OracleState, band) -> np.ndarray:
+    """Pad a compact (N, N/2) band like STEP2A, zero the kz=-N/2 row, irfft2."""
+    N, Nh, M = S.N, S.Nh, S.M
+    tmp = np.zeros((M, S.NK_full), S.cdt)
+    tmp[:N, :Nh] = band
+    tmp[:, Nh:min(3 * N // 4, S.NK_full - 1) + 1] = 0
+    tmp[N:N + Nh, :Nh] = tmp[Nh:N, :Nh]
+    tmp[Nh:N, :Nh] = 0
+    tmp[N, :Nh] = 0
+    return spfft.irfft2(tmp, s=(M, M), axes=(0, 1), norm="forward", workers=S.workers)
+
+
+def om2_phys(S: OracleState) -> np.ndarray:
+    return band_to_phys(S, S.om2)
+
+
+def stream_func(S: OracleState) -> np.ndarray:
+    K2 = S.K2 + S.rdt.type(1.0e-30)
+    return band_to_phys(S, S.om2 / K2)
+
+
+def kinetic(S: OracleState) -> np.ndarray:
+    u, w = S.ur_full[0], S.ur_full[1]
+    return np.sqrt(u * u + w * w)
+
+
+def to_pixels(field) -> np.ndarray:
+    """8-bit frame as turbo_wrapper.py:317-351 (1..255, 128 if constant)."""
+    f = np.asarray(field, np.float64)
+    lo, hi = f.min(), f.max()
+    if abs(hi - lo) <= 1e-12:
+        return np.full(f.shape, 128, np.uint8)
+    return np.clip(1.0 + (f - lo) / (hi - lo) * 254.0, 1.0, 255.0).astype(np.uint8)

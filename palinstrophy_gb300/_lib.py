@@ -65,6 +65,8 @@ _SIGS = {
     "pal_next_dt": (_I, [_H, _I, _DP]),
     "pal_diagnostics": (_I, [_H, ctypes.POINTER(PalDiag)]),
     "pal_get_field": (_I, [_H, _I, _P]),
+    "pal_vis_field": (_I, [_H, _I, _P, ctypes.POINTER(ctypes.c_ubyte)]),
+    "pal_energy_spectrum": (_I, [_H, _I, _D, _D, _DP, ctypes.POINTER(_I)]),
     "pal_field_device_ptr": (_I, [_H, _I, ctypes.POINTER(_P)]),
     "pal_materialize_physical": (_I, [_H]),
     "pal_synchronize": (_I, [_H]),

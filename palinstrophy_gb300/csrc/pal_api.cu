@@ -46,6 +46,8 @@ struct pal_handle {
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
   void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
+  void *vis_w = nullptr;      // two scratch work planes for display transforms
+  void *vis_phys = nullptr;   // three physical planes (u|scalar, v, |u|)
   DevScalars* sc = nullptr;
   DevScalars* sc_host = nullptr;  // pinned mirror
   double* part = nullptr;
@@ -353,7 +355,8 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
 int pal_destroy(pal_handle* h) {
   if (!h) return PAL_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* bufs[] = {h->w0, h->w1, h->om, h->fnm1, h->stage, h->tw_row, h->tw_col, h->phys, h->sc, h->part};
+  void* bufs[] = {h->w0,     h->w1,   h->om,   h->fnm1, h->stage, h->tw_row,
+                  h->tw_col, h->phys, h->sc,   h->part, h->vis_w, h->vis_phys};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -540,6 +543,78 @@ int pal_diagnostics(pal_handle* h, pal_diag* out) {
   out->energy_joules = 0.5 * (2.0 * pal::kPi) * (2.0 * pal::kPi) * s->mean_speed2;
   out->nonfinite = s->nonfinite;
   if (s->nonfinite) return fail(h, PAL_ERR_NONFINITE, "NaN/Inf in the field");
+  return PAL_OK;
+}
+
+int pal_energy_spectrum(pal_handle* h, int nbins, double r_max, double k_nyq, double* esum, int* count) {
+  if (int rc = check(h)) return rc;
+  if (nbins <= 0 || !(r_max > 0.0) || !(k_nyq > 0.0) || !esum || !count)
+    return fail(h, PAL_ERR_INVALID, "bad spectrum arguments");
+  if (h->state == ST_EMPTY) return fail(h, PAL_ERR_STATE, "no spectral state set");
+  double* d_e = nullptr;
+  PAL_CK(h, cudaMallocAsync(reinterpret_cast<void**>(&d_e), (size_t)nbins * (sizeof(double) + sizeof(int)),
+                            h->stream));
+  int* d_c = reinterpret_cast<int*>(d_e + nbins);
+  const double scale = (double)h->M * (double)h->M;
+  h->ks->spectrum(h->om, h->N, nbins, r_max, k_nyq, scale * scale, d_e, d_c, h->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(esum, d_e, nbins * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(count, d_c, nbins * sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  cudaFreeAsync(d_e, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "energy spectrum");
+  return PAL_OK;
+}
+
+int pal_vis_field(pal_handle* h, int var, void* host_field, unsigned char* host_pixels) {
+  if (int rc = check(h)) return rc;
+  if (var < PAL_VAR_U || var > PAL_VAR_STREAM) return fail(h, PAL_ERR_INVALID, "unknown display variable");
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "display between step2b and step3");
+  const size_t rsz = h->esz / 2;
+  const long long plane = (long long)h->M * h->M;
+  // scratch: 3 physical planes, then [DevScalars | min,max | counter | 512 x (min,max) partials | pixels]
+  const size_t aux = 256 + 16 + 16 + 512 * 16;
+  if (!h->vis_phys) PAL_CK(h, cudaMalloc(&h->vis_phys, 3 * plane * rsz + aux + plane));
+  char* auxp = static_cast<char*>(h->vis_phys) + 3 * plane * rsz;
+  DevScalars* vsc = reinterpret_cast<DevScalars*>(auxp);
+  double* mm = reinterpret_cast<double*>(auxp + 256);
+  unsigned int* counter = reinterpret_cast<unsigned int*>(auxp + 256 + 16);
+  double* mm_part = reinterpret_cast<double*>(auxp + 256 + 32);
+  unsigned char* d_pix = reinterpret_cast<unsigned char*>(auxp + aux);
+  PAL_CK(h, cudaMemsetAsync(auxp, 0, 256 + 32, h->stream));
+  StepArgs a = base_args(h);
+  a.phys = h->vis_phys;
+  a.sc = vsc;  // display statistics never touch the state's scalars
+  a.flags = pal::F_PHYS | pal::F_STATS;
+  if (var == PAL_VAR_OMEGA || var == PAL_VAR_STREAM) {
+    if (!h->vis_w) PAL_CK(h, cudaMalloc(&h->vis_w, 2 * (size_t)h->Nh * h->M * h->esz));
+    StepArgs b = base_args(h);
+    b.w0 = h->vis_w;
+    b.w1 = static_cast<char*>(h->vis_w) + (size_t)h->Nh * h->M * h->esz;
+    b.tw = h->tw_col;
+    b.scheme = var == PAL_VAR_OMEGA ? 1 : 2;
+    h->ck->col_inv(b, h->stream);
+    PAL_LAUNCHED(h, "k_col_inv (display)");
+    a.w0 = b.w0;
+    a.w1 = b.w1;
+  }
+  h->rk->phys(a, h->stream);
+  PAL_LAUNCHED(h, "k_phys (display)");
+  const char* src = static_cast<const char*>(h->vis_phys);
+  if (var == PAL_VAR_V) src += plane * rsz;
+  if (var == PAL_VAR_ENERGY) {
+    h->ks->speed(h->vis_phys, plane, h->stream);
+    PAL_LAUNCHED(h, "k_speed");
+    src += 2 * plane * rsz;
+  }
+  if (host_field) PAL_CK(h, cudaMemcpyAsync(host_field, src, plane * rsz, cudaMemcpyDeviceToHost, h->stream));
+  if (host_pixels) {
+    h->ks->pixels(src, plane, mm_part, counter, mm, d_pix, h->stream);
+    PAL_LAUNCHED(h, "k_pixels");
+    PAL_CK(h, cudaMemcpyAsync(host_pixels, d_pix, plane, cudaMemcpyDeviceToHost, h->stream));
+  }
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
   return PAL_OK;
 }
 

@@ -636,7 +636,20 @@ __global__ void __launch_bounds__(NT) k_col_inv(StepArgs a0) {
     C val = {T(0), T(0)};
     if (f < Nh || f >= N) {
       const int z = f < Nh ? f : f - Nh;
-      if (src != nullptr) {
+      if (a.scheme != 0) {
+        // scalar band for display (turbo_simulator.py:2639-2709): omega, or the
+        // streamfunction omega/(K2 + 1e-30); the kz = -N/2 row is left out
+        if (v == 0 && z != Nh) {
+          const C o = om[z];
+          if (a.scheme == 1) {
+            val = o;
+          } else {
+            const T gz = T(z < Nh ? z : z - N);
+            const T ik = T(1) / (T(kx) * T(kx) + gz * gz + T(1.0e-30));
+            val = C{o.x * ik, o.y * ik};
+          }
+        }
+      } else if (src != nullptr) {
         val = src[(size_t)v * N * Nh + (size_t)z * Nh + kx];
       } else {
         const C o = om[z];
@@ -721,6 +734,110 @@ __global__ void __launch_bounds__(NT) k_spectral(StepArgs a0) {
     sc->P = t[3];
     sc->kmax2 = double(Nh - 1) * double(Nh - 1) + double(Nh) * double(Nh);
     sc->diag_counter = 0u;
+  }
+}
+
+// Energy spectrum of the compact vorticity band (turbo_simulator.py:2225-2357):
+// mode (kx, kz), K2 > 0, goes to bin floor((sqrt(K2)/k_nyq / r_max) nbins)
+// (clipped) with p = |om|^2 / K2 * scale2, doubled (and counted twice) for
+// kx > 0.  One block per bin: its threads walk the rows kz and only visit the
+// kx interval of that bin's annulus (float estimate plus a one-mode margin),
+// testing each mode with the reference's double-precision formula, so every
+// mode is counted exactly once and the sums are deterministic.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_spectrum(const cplx<T>* __restrict__ om, int N, int nbins, double r_max,
+                                                 double k_nyq, double scale2, double* __restrict__ esum,
+                                                 int* __restrict__ cnt) {
+  const int b = blockIdx.x;
+  const int Nh = N >> 1;
+  const float c = (float)(k_nyq * r_max / (double)nbins);  // annulus width in k
+  const float lo = b * c, hi = (b == nbins - 1) ? 3.0e38f : (b + 1) * c;
+  double e = 0.0;
+  long long n = 0;
+  for (int z = threadIdx.x; z < N; z += NT) {
+    const int kz = z < Nh ? z : z - N;
+    const float kz2 = (float)kz * (float)kz;
+    const float a = lo * lo - kz2;
+    int x0 = a > 0.f ? (int)floorf(sqrtf(a)) - 1 : 0;
+    const float h = hi * hi - kz2;
+    if (h < 0.f) continue;
+    int x1 = (hi > 1.0e37f) ? Nh - 1 : (int)ceilf(sqrtf(h)) + 1;
+    x0 = max(x0, 0);
+    x1 = min(x1, Nh - 1);
+    for (int kx = x0; kx <= x1; ++kx) {
+      const double k2 = (double)kx * (double)kx + (double)kz * (double)kz;
+      if (!(k2 > 0.0)) continue;
+      const double r = sqrt(k2) / k_nyq;
+      int bin = (int)floor((r / r_max) * (double)nbins);
+      bin = bin < 0 ? 0 : (bin >= nbins ? nbins - 1 : bin);
+      if (bin != b) continue;
+      const cplx<T> o = om[(size_t)kx * N + z];
+      double p = (((double)o.x * (double)o.x + (double)o.y * (double)o.y) / k2) * scale2;
+      const int wgt = kx > 0 ? 2 : 1;
+      if (wgt == 2) p *= 2.0;
+      e += p;
+      n += wgt;
+    }
+  }
+  __shared__ double red[2 * (NT / 32)];
+  double v[2] = {e, (double)n};
+  block_sum<NT, 2>(v, red, threadIdx.x);
+  if (threadIdx.x == 0) {
+    esum[b] = v[0];
+    cnt[b] = (int)v[1];
+  }
+}
+
+// Display fields: |u| from the physical planes, then min/max normalisation to
+// 8-bit pixels 1..255 (128 for a constant field) as turbo_wrapper.py:317-351.
+template <typename T>
+__global__ void k_speed(T* __restrict__ ph, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T u = ph[i], v = ph[n + i];
+    ph[2 * n + i] = sqrt(u * u + v * v);
+  }
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_minmax(const T* __restrict__ f, long long n, double* part, unsigned int* counter,
+                                                double* out) {
+  double mn = 1e300, mx = -1e300;
+  for (long long i = (long long)blockIdx.x * NT + threadIdx.x; i < n; i += (long long)gridDim.x * NT) {
+    const double x = (double)f[i];
+    mn = fmin(mn, x);
+    mx = fmax(mx, x);
+  }
+  __shared__ double red[NT / 32];
+  mx = block_max<NT>(mx, red, threadIdx.x);
+  mn = -block_max<NT>(-mn, red, threadIdx.x);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = mn;
+    part[2 * blockIdx.x + 1] = mx;
+  }
+  if (!last_block(counter, threadIdx.x)) return;
+  double a = 1e300, b = -1e300;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += NT) {
+    a = fmin(a, __ldcg(part + 2 * q));
+    b = fmax(b, __ldcg(part + 2 * q + 1));
+  }
+  b = block_max<NT>(b, red, threadIdx.x);
+  a = -block_max<NT>(-a, red, threadIdx.x);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+    *counter = 0u;
+  }
+}
+
+template <typename T>
+__global__ void k_pixels(const T* __restrict__ f, long long n, const double* mm, unsigned char* __restrict__ pix) {
+  const double mn = mm[0], rng = mm[1] - mm[0];
+  const bool flat = fabs(rng) <= 1.0e-12;
+  const T fmn = (T)mn, frng = (T)(flat ? 1.0 : rng);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T p = T(1) + (f[i] - fmn) / frng * T(254);
+    p = p < T(1) ? T(1) : (p > T(255) ? T(255) : p);
+    pix[i] = flat ? (unsigned char)128 : (unsigned char)p;
   }
 }
 

@@ -41,6 +41,12 @@ struct KernelSet {
   int n_cols;
   void (*spectral)(const StepArgs&, cudaStream_t, int blocks);
   void (*transpose)(const void* in, void* out, int rows, int cols, int batch, cudaStream_t);
+  void (*spectrum)(const void* om, int N, int nbins, double r_max, double k_nyq, double scale2, double* esum, int* cnt,
+                   cudaStream_t);
+  // display: |u| into plane 2 of `phys`, and min/max -> 8-bit pixels of one plane
+  void (*speed)(void* phys, long long plane, cudaStream_t);
+  void (*pixels)(const void* plane, long long n, double* part, unsigned int* counter, double* mm, unsigned char* pix,
+                 cudaStream_t);
 };
 
 constexpr int kSpectralThreads = 256;
@@ -106,6 +112,25 @@ void launch_transpose(const void* in, void* out, int rows, int cols, int batch, 
                                               cols);
 }
 
+template <typename T>
+void launch_spectrum(const void* om, int N, int nbins, double r_max, double k_nyq, double scale2, double* esum,
+                     int* cnt, cudaStream_t s) {
+  k_spectrum<T, 256><<<nbins, 256, 0, s>>>(static_cast<const cplx<T>*>(om), N, nbins, r_max, k_nyq, scale2, esum,
+                                             cnt);
+}
+
+template <typename T>
+void launch_speed(void* phys, long long plane, cudaStream_t s) {
+  k_speed<T><<<1024, 256, 0, s>>>(static_cast<T*>(phys), plane);
+}
+
+template <typename T>
+void launch_pixels(const void* plane, long long n, double* part, unsigned int* counter, double* mm, unsigned char* pix,
+                   cudaStream_t s) {
+  k_minmax<T, 256><<<512, 256, 0, s>>>(static_cast<const T*>(plane), n, part, counter, mm);
+  k_pixels<T><<<1024, 256, 0, s>>>(static_cast<const T*>(plane), n, mm, pix);
+}
+
 #define PAL_KERNEL_SET(T, PREC, N, ROWS, COLS)                                                          \
   static const ::pal::KernelSet kSet##N = {N,                                                           \
                                            3 * (N) / 2,                                                 \
@@ -115,7 +140,10 @@ void launch_transpose(const void* in, void* out, int rows, int cols, int batch, 
                                            COLS,                                                        \
                                            (int)(sizeof(COLS) / sizeof(COLS[0])),                       \
                                            ::pal::launch_spectral<T>,                                   \
-                                           ::pal::launch_transpose<T>};
+                                           ::pal::launch_transpose<T>,                                  \
+                                           ::pal::launch_spectrum<T>,                                   \
+                                           ::pal::launch_speed<T>,                                      \
+                                           ::pal::launch_pixels<T>};
 
 }  // namespace pal
 

@@ -192,6 +192,21 @@ class Field:
         self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_UR_U if comp == 0 else L.PAL_FIELD_UR_V, L.ptr(a)))
         return a
 
+    def vis(self, var: int, field: bool = True, pixels: bool = False):
+        """Display field var (VAR_U..VAR_STREAM): (float field or None, uint8 pixels or None)."""
+        f = np.empty((self.M, self.M), self.rdt) if field else None
+        p = np.empty((self.M, self.M), np.uint8) if pixels else None
+        self._ck(self.lib.pal_vis_field(self.h, int(var), None if f is None else L.ptr(f),
+                                        None if p is None else p.ctypes.data_as(L.ctypes.POINTER(L.ctypes.c_ubyte))))
+        return f, p
+
+    def energy_spectrum(self, nbins: int, r_max: float, k_nyq: float):
+        e = np.zeros(nbins, np.float64)
+        c = np.zeros(nbins, np.int32)
+        self._ck(self.lib.pal_energy_spectrum(self.h, int(nbins), float(r_max), float(k_nyq),
+                                              e.ctypes.data_as(L._DP), c.ctypes.data_as(L.ctypes.POINTER(L._I))))
+        return e, c
+
     def device_ptr(self, which: int) -> int:
         p = L._P()
         self._ck(self.lib.pal_field_device_ptr(self.h, which, L.ctypes.byref(p)))
@@ -314,6 +329,29 @@ def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float 
     S.visc = float(st["visc"])
     S.dt, S.cn, S.cnm1 = 0.0, 1.0, 0.0
     return S
+
+
+VAR_U, VAR_V, VAR_ENERGY, VAR_OMEGA, VAR_STREAM = 0, 1, 2, 3, 4
+
+
+def dns_kinetic(S: DnsState):
+    """|u| on the 3/2 grid (turbo_simulator.py:2629-2636); returned, not stored in ur_full[2]."""
+    return S.field.vis(VAR_ENERGY)[0]
+
+
+def dns_om2_phys(S: DnsState):
+    """Physical vorticity from om2 (turbo_simulator.py:2684-2687)."""
+    return S.field.vis(VAR_OMEGA)[0]
+
+
+def dns_stream_func(S: DnsState):
+    """Streamfunction om2/(K2 + 1e-30) on the 3/2 grid (turbo_simulator.py:2690-2708)."""
+    return S.field.vis(VAR_STREAM)[0]
+
+
+def frame_pixels(S: DnsState, var: int = VAR_U):
+    """uint8 display frame of DnsSimulator's variable selector (turbo_wrapper.py:353-413)."""
+    return S.field.vis(var, field=False, pixels=True)[1]
 
 
 def dns_step2a(S: DnsState) -> None:
@@ -512,3 +550,20 @@ class Ensemble:
 
     def synchronize(self):
         self._ck(self.lib.pal_ensemble_synchronize(self.h))
+
+
+# Spectrum API of the reference module (turbo_simulator.py:2225-2622).
+from .spectrum import (  # noqa: E402,F401
+    SpectrumAverageState,
+    SpectrumSample,
+    compute_energy_spectrum_uv_bins,
+    initialize_spectrum_average_from_sample,
+    mark_spectrum_average_since_restart,
+    sample_and_update_spectrum_average,
+    save_energy_spectrum_csv_data,
+    save_energy_spectrum_uv_csv,
+    save_spectrum_average_csv,
+    spectrum_average_kind,
+    spectrum_average_mean_energy,
+    update_spectrum_average,
+)

@@ -328,3 +328,74 @@ def test_every_kernel_candidate_agrees(ts, prec, tol, N):
             do.rk3(S)
         assert do.rel_l2(S.om2, ref) <= tol
     F.close()
+
+
+@pytest.mark.parametrize("N,prec,tol", [(64, "fp64", 1e-12), (256, "fp64", 1e-12), (256, "fp32", 1e-6)])
+def test_energy_spectrum_matches_oracle(ts, N, prec, tol):
+    """Shell bins of |om|^2/K2 (GPU, deterministic) against the oracle's bincount."""
+    from palinstrophy_gb300 import spectrum as sp
+    g = pg.generate(N, 10.0, 1e4, 4895, "KM3") if N <= 64 else None
+    if g is None:
+        d = golden("init_KM3_N256_s4895_k10.npz")
+        om2, uc, visc = d["om2"], d["uc_low"], float(d["visc"])
+    else:
+        om2, uc, visc = g["om2"], g["uc_low"], float(g["visc"])
+    F, S = _pair(ts, N, prec, om2, uc, visc, 0.5)
+    _gpu_init_dt(F)
+    do.init_dt(S)
+    F.step("CNAB2", 3, update=0)
+    for _ in range(3):
+        do.cnab2(S)
+    s1 = sp.compute_energy_spectrum_uv_bins(F)
+    s2 = sp.compute_energy_spectrum_uv_bins(F)
+    assert np.array_equal(s1.energy, s2.energy)  # deterministic
+    e_ref, c_ref = do.omega_spectrum_bins(S)
+    assert np.array_equal(s1.count, c_ref)
+    m = e_ref > 0
+    if prec == "fp64":  # every bin to double rounding
+        assert np.max(np.abs(s1.energy[m] - e_ref[m]) / e_ref[m]) <= tol
+    else:  # FP32 field: the spectrum as a whole
+        assert np.abs(s1.energy - e_ref).sum() / e_ref.sum() <= tol
+    assert s1.nbins == max(32, 2 * N)
+    F.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-6)])
+def test_display_fields_match_oracle(ts, prec, tol):
+    """u, v, |u|, omega, streamfunction on the 3/2 grid and their 8-bit frames;
+    the display passes must leave the simulation state untouched."""
+    om2, uc, visc = _init("init_KM3_N64_s4895_k10.npz")
+    F, S = _pair(ts, 64, prec, om2, uc, visc, 0.5)
+    _gpu_init_dt(F)
+    do.init_dt(S)
+    F.step("CNAB2", 4, update=0)
+    for _ in range(4):
+        do.cnab2(S)
+    before = F.om2()
+    refs = {0: S.ur_full[0], 1: S.ur_full[1], 2: do.kinetic(S), 3: do.om2_phys(S), 4: do.stream_func(S)}
+    for var, ref in refs.items():
+        f, pix = F.vis(var, field=True, pixels=True)
+        err = np.linalg.norm(f.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert err <= tol, (var, err)
+        rp = do.to_pixels(ref)
+        assert np.mean(np.abs(pix.astype(int) - rp.astype(int)) <= 1) > 0.999, var
+    assert np.array_equal(before, F.om2())
+    d = F.diagnostics()
+    U, _, _ = do.flow_eddy_metrics(S)
+    assert abs(d["U"] - U) <= 1e-5 * U
+    F.close()
+
+
+def test_k4_start_runs(ts):
+    from palinstrophy_gb300.initial import k4_unit_energy
+    om2, uc = k4_unit_energy(256, 15.0, 4895)
+    F = ts.Field(256, "fp32", 1e4, 0.1)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", 1e-4)
+    _gpu_init_dt(F)
+    d0 = F.diagnostics()
+    # Parseval: mean(u^2 + v^2) on the 3/2 grid equals the unit energy measure
+    assert abs(d0["U"] ** 2 - 1.0) < 1e-5
+    F.step("LS_IMEX_RK3", 5, update=1, final_update=True)
+    assert F.diagnostics()["nonfinite"] == 0
+    F.close()

@@ -131,6 +131,17 @@ int pal_energy_spectrum(pal_handle* h, int nbins, double r_max, double k_nyq, do
  * so the simulation state is unchanged.  Waits. */
 int pal_vis_field(pal_handle* h, int var, void* host_field, unsigned char* host_pixels);
 
+/* Gradient of the final palinstrophy L = 1/2 sum w' K2 |om|^2 (w' = 1 for kx = 0,
+ * else 2: 1/2 <|grad omega|^2> on the grid) after nsteps LS-IMEX-RK3 steps at
+ * the handle's fixed dt (no NEXTDT), with respect to the current om2 (the
+ * velocity is taken as its inversion).  Hand-written discrete adjoint of the
+ * stage (transposed padded transforms, adjoint products and inversion, reversed
+ * IMEX stages), states checkpointed every ckpt_every steps and recomputed.
+ * grad_host receives dL/d(om2) in the reference layout (real inner product
+ * Re sum conj(g) d om2); the handle ends at the final forward state.  The
+ * reference has no differentiation; N = 32..512.  Waits. */
+int pal_adjoint_palinstrophy(pal_handle* h, int nsteps, int ckpt_every, double* loss, void* grad_host);
+
 /* Copy a field to host memory in the reference layout (waits). */
 int pal_get_field(pal_handle* h, int which, void* host_dst);
 /* Device pointer of a field: om2/fnm1 are stored transposed, [kx][z] (N/2 x N);

@@ -65,6 +65,7 @@ _SIGS = {
     "pal_next_dt": (_I, [_H, _I, _DP]),
     "pal_diagnostics": (_I, [_H, ctypes.POINTER(PalDiag)]),
     "pal_get_field": (_I, [_H, _I, _P]),
+    "pal_adjoint_palinstrophy": (_I, [_H, _I, _I, _DP, _P]),
     "pal_vis_field": (_I, [_H, _I, _P, ctypes.POINTER(ctypes.c_ubyte)]),
     "pal_energy_spectrum": (_I, [_H, _I, _D, _D, _DP, ctypes.POINTER(_I)]),
     "pal_field_device_ptr": (_I, [_H, _I, ctypes.POINTER(_P)]),

@@ -7,6 +7,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <map>
@@ -616,6 +617,120 @@ int pal_vis_field(pal_handle* h, int var, void* host_field, unsigned char* host_
   }
   PAL_CK(h, cudaStreamSynchronize(h->stream));
   return PAL_OK;
+}
+
+int pal_adjoint_palinstrophy(pal_handle* h, int nsteps, int ckpt_every, double* loss, void* grad_host) {
+  if (int rc = check(h)) return rc;
+  const pal::AdjKernels* adj = h->ks->adj;
+  if (!adj) return fail(h, PAL_ERR_INVALID, "no adjoint kernels compiled for this grid");
+  if (nsteps <= 0 || ckpt_every <= 0) return fail(h, PAL_ERR_INVALID, "nsteps and ckpt_every must be positive");
+  if (int rc = resolve_velocity(h)) return rc;
+  if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "adjoint needs the physical velocity");
+  if (adj->configure() != cudaSuccess) return fail(h, PAL_ERR_CUDA, "adjoint configure");
+  const size_t plane_om = (size_t)h->Nh * h->N * h->esz, plane_w = (size_t)h->Nh * h->M * h->esz;
+  const int n_ck = (nsteps + ckpt_every - 1) / ckpt_every;
+  const int stages_max = 3 * ckpt_every;
+  // one allocation: checkpoints (om, fnm1) | final state | stage inputs | lam_om, lam_f | Y planes | tables | loss
+  const size_t tw_bytes = (size_t)(adj->tw_row_elems + adj->tw_col_elems) * h->esz;
+  const int seed_blocks = 256;
+  const size_t bytes = 2 * plane_om * (size_t)n_ck + 2 * plane_om + plane_om * (size_t)stages_max + 2 * plane_om +
+                       2 * plane_w + tw_bytes + seed_blocks * sizeof(double) + 1024;
+  char* buf = nullptr;
+  PAL_CK(h, cudaMallocAsync(reinterpret_cast<void**>(&buf), bytes, h->stream));
+  char* ck = buf;
+  char* fin = ck + 2 * plane_om * (size_t)n_ck;
+  char* st = fin + 2 * plane_om;
+  char* lom = st + plane_om * (size_t)stages_max;
+  char* lf = lom + plane_om;
+  char* y0 = lf + plane_om;
+  char* y1 = y0 + plane_w;
+  char* tw_r = y1 + plane_w;
+  char* tw_c = tw_r + (size_t)adj->tw_row_elems * h->esz;
+  double* loss_part = reinterpret_cast<double*>(((uintptr_t)(tw_c + (size_t)adj->tw_col_elems * h->esz) + 255) & ~(uintptr_t)255);
+  adj->tw_row(tw_r, h->stream);
+  adj->tw_col(tw_c, h->stream);
+  int rc = PAL_OK;
+  auto seg_len = [&](int seg) { return std::min(ckpt_every, nsteps - seg * ckpt_every); };
+  // forward sweep with checkpoints (fixed dt: no NEXTDT)
+  for (int seg = 0; seg < n_ck && rc == PAL_OK; ++seg) {
+    cudaMemcpyAsync(ck + 2 * plane_om * seg, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(ck + 2 * plane_om * seg + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    for (int j = 0; j < seg_len(seg) && rc == PAL_OK; ++j) rc = one_step(h, PAL_LS_IMEX_RK3, false, true);
+  }
+  if (rc) {
+    cudaFreeAsync(buf, h->stream);
+    return rc;
+  }
+  cudaMemcpyAsync(fin, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(fin + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+  adj->seed(h->om, lom, lf, h->N, loss_part, seed_blocks, h->stream);
+  // backward sweep: per segment, recompute and store the stage inputs, then run
+  // the adjoint stages in reverse
+  for (int seg = n_ck - 1; seg >= 0 && rc == PAL_OK; --seg) {
+    cudaMemcpyAsync(h->om, ck + 2 * plane_om * seg, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(h->fnm1, ck + 2 * plane_om * seg + plane_om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    h->state = ST_VEL_PENDING;
+    h->vel_uploaded = false;
+    if ((rc = resolve_velocity(h))) break;
+    const int ns = seg_len(seg);
+    for (int j = 0; j < ns && rc == PAL_OK; ++j) {
+      for (int s = 0; s < 3 && rc == PAL_OK; ++s) {
+        cudaMemcpyAsync(st + plane_om * (size_t)(3 * j + s), h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+        if ((rc = launch_row(h, 0))) break;
+        rc = launch_col(h, 1, s, 0);
+      }
+    }
+    for (int q = 3 * ns - 1; q >= 0 && rc == PAL_OK; --q) {
+      const int s = q % 3;
+      StepArgs a = base_args(h);
+      a.om = lom;
+      a.fnm1 = lf;
+      a.alpha = kRkAlpha[s];
+      a.beta = kRkBeta[s];
+      a.tw = tw_c;
+      adj->col_in(a, h->stream);
+      StepArgs b = base_args(h);
+      b.om = st + plane_om * (size_t)q;
+      b.w0 = y0;
+      b.w1 = y1;
+      b.tw = tw_c;
+      b.src = nullptr;
+      adj->col_vel(b, h->stream);
+      a.y0 = y0;
+      a.y1 = y1;
+      a.tw = tw_r;
+      adj->row(a, h->stream);
+      a.tw = tw_c;
+      adj->col_out(a, h->stream);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = cuda_fail(h, e, "adjoint stage");
+    }
+  }
+  // leave the handle at the final forward state
+  cudaMemcpyAsync(h->om, fin, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+  cudaMemcpyAsync(h->fnm1, fin + plane_om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+  h->state = ST_VEL_PENDING;
+  h->vel_uploaded = false;
+  if (rc == PAL_OK) rc = resolve_velocity(h);
+  if (rc == PAL_OK && grad_host) {
+    h->ks->transpose(lom, h->stage, h->Nh, h->N, 1, h->stream);
+    cudaError_t e = cudaMemcpyAsync(grad_host, h->stage, plane_om, cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "gradient download");
+  }
+  std::vector<double> lp(seed_blocks, 0.0);
+  if (rc == PAL_OK && loss) {
+    cudaError_t e = cudaMemcpyAsync(lp.data(), loss_part, seed_blocks * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "loss download");
+  }
+  cudaFreeAsync(buf, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (rc == PAL_OK && e != cudaSuccess) rc = cuda_fail(h, e, "adjoint");
+  if (rc == PAL_OK && loss) {
+    double acc = 0.0;
+    for (double v : lp) acc += v;
+    *loss = acc;
+  }
+  return rc;
 }
 
 int pal_materialize_physical(pal_handle* h) {

@@ -44,12 +44,12 @@ const RowKernels r768[] = {RowOf<float, P1152, 4, 256>::make("8.6.24 V4x256"),
 const ColKernels c768[] = {ColOf<float, P1152, 256>::make("8.6.24 x256"), ColOf<float, P1152, 128>::make("8.6.24 x128"),
                            ColOf<float, P1152b, 256>::make("12.4.24 x256")};
 
-PAL_KERNEL_SET(float, 0, 32, r32, c32)
-PAL_KERNEL_SET(float, 0, 64, r64, c64)
-PAL_KERNEL_SET(float, 0, 128, r128, c128)
-PAL_KERNEL_SET(float, 0, 256, r256, c256)
+PAL_KERNEL_SET_ADJ(float, 0, 32, r32, c32, (AdjOf<float, P48, 4, 64, P48, 64>::get()))
+PAL_KERNEL_SET_ADJ(float, 0, 64, r64, c64, (AdjOf<float, P96, 4, 128, P96, 64>::get()))
+PAL_KERNEL_SET_ADJ(float, 0, 128, r128, c128, (AdjOf<float, P192, 4, 128, P192, 64>::get()))
+PAL_KERNEL_SET_ADJ(float, 0, 256, r256, c256, (AdjOf<float, P384, 4, 256, P384, 128>::get()))
 PAL_KERNEL_SET(float, 0, 384, r384, c384)
-PAL_KERNEL_SET(float, 0, 512, r512, c512)
+PAL_KERNEL_SET_ADJ(float, 0, 512, r512, c512, (AdjOf<float, P768, 4, 256, P768, 128>::get()))
 PAL_KERNEL_SET(float, 0, 768, r768, c768)
 }  // namespace
 

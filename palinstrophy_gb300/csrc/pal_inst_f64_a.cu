@@ -32,12 +32,12 @@ const RowKernels r1024[] = {RowOf<double, P1536, 2, 256>::make("16.6.16 V2x256")
                             RowOf<double, P1536, 1, 128>::make("16.6.16 V1x128")};
 const ColKernels c1024[] = {ColOf<double, P1536, 256>::make("16.6.16 x256"), ColOf<double, P1536, 128>::make("16.6.16 x128")};
 
-PAL_KERNEL_SET(double, 1, 32, r32, c32)
-PAL_KERNEL_SET(double, 1, 64, r64, c64)
-PAL_KERNEL_SET(double, 1, 128, r128, c128)
-PAL_KERNEL_SET(double, 1, 256, r256, c256)
+PAL_KERNEL_SET_ADJ(double, 1, 32, r32, c32, (AdjOf<double, P48, 2, 64, P48, 64>::get()))
+PAL_KERNEL_SET_ADJ(double, 1, 64, r64, c64, (AdjOf<double, P96, 2, 64, P96, 64>::get()))
+PAL_KERNEL_SET_ADJ(double, 1, 128, r128, c128, (AdjOf<double, P192, 2, 128, P192, 64>::get()))
+PAL_KERNEL_SET_ADJ(double, 1, 256, r256, c256, (AdjOf<double, P384, 2, 256, P384, 128>::get()))
 PAL_KERNEL_SET(double, 1, 384, r384, c384)
-PAL_KERNEL_SET(double, 1, 512, r512, c512)
+PAL_KERNEL_SET_ADJ(double, 1, 512, r512, c512, (AdjOf<double, P768, 2, 256, P768, 128>::get()))
 PAL_KERNEL_SET(double, 1, 768, r768, c768)
 PAL_KERNEL_SET(double, 1, 1024, r1024, c1024)
 }  // namespace

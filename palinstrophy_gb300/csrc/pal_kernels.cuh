@@ -62,6 +62,8 @@ struct StepArgs {
   // advances by its stride (in elements) and sc by one DevScalars per member.
   int members;      // grid.y of the launch (>= 1)
   long long ms_w, ms_om, ms_part, ms_phys, ms_src;
+  const void* y0;   // adjoint: the forward velocity planes of the stage
+  const void* y1;
 };
 
 // Member view of the arguments for block row blockIdx.y.
@@ -183,13 +185,14 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, int M, in
 // Z[k] = u^[k] + i v^[k] (k < N/2; real parts only at k = 0),
 // Z[M-k] = conj(u^[k]) + i conj(v^[k]), zero elsewhere (the 3/2 pad).
 template <typename T, class PL, int V, int NT>
-__device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, int z0, int tid) {
+__device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, int z0, int tid,
+                                               const void* p0 = nullptr, const void* p1 = nullptr) {
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int R = PL::R[0];
   constexpr int S = M / R;
-  const C* __restrict__ w0 = static_cast<const C*>(a.w0);
-  const C* __restrict__ w1 = static_cast<const C*>(a.w1);
+  const C* __restrict__ w0 = static_cast<const C*>(p0 ? p0 : a.w0);
+  const C* __restrict__ w1 = static_cast<const C*>(p1 ? p1 : a.w1);
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   constexpr int Nh = M / 3;
   for (int w = tid; w < V * S; w += NT) {

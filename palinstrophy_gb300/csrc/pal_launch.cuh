@@ -7,6 +7,7 @@
 // twiddle tables.  pal_create times every candidate on the handle's own state
 // and keeps the fastest (pal_autotune in pal_api.cu).
 #pragma once
+#include "pal_adjoint.cuh"
 #include "pal_kernels.cuh"
 
 namespace pal {
@@ -33,6 +34,19 @@ struct ColKernels {
   void (*twiddles)(void* tw, cudaStream_t);
 };
 
+// Adjoint of one LS-IMEX-RK3 stage (pal_adjoint.cuh), on fixed plans.
+struct AdjKernels {
+  int tw_row_elems, tw_col_elems;
+  cudaError_t (*configure)();
+  void (*col_in)(const StepArgs&, cudaStream_t);
+  void (*row)(const StepArgs&, cudaStream_t);
+  void (*col_out)(const StepArgs&, cudaStream_t);
+  void (*col_vel)(const StepArgs&, cudaStream_t);  // the stage's velocity planes from om_in
+  void (*tw_row)(void* tw, cudaStream_t);
+  void (*tw_col)(void* tw, cudaStream_t);
+  void (*seed)(const void* om, void* lom, void* lf, int N, double* loss_part, int blocks, cudaStream_t);
+};
+
 struct KernelSet {
   int N, M, precision;
   const RowKernels* rows;
@@ -47,6 +61,7 @@ struct KernelSet {
   void (*speed)(void* phys, long long plane, cudaStream_t);
   void (*pixels)(const void* plane, long long n, double* part, unsigned int* counter, double* mm, unsigned char* pix,
                  cudaStream_t);
+  const AdjKernels* adj;  // nullptr where no adjoint is compiled
 };
 
 constexpr int kSpectralThreads = 256;
@@ -100,6 +115,41 @@ struct ColOf {
   }
 };
 
+template <typename T, class PLR, int V, int NTR, class PLC, int NTC>
+struct AdjOf {
+  static constexpr size_t smem_row = size_t(PLR::PADM) * V * sizeof(cplx<T>) * 2;
+  static constexpr size_t smem_col = size_t(PLC::PADM) * 2 * sizeof(cplx<T>);
+  static_assert(smem_row <= kSmemLimit && smem_col <= kSmemLimit, "adjoint tiles do not fit");
+  static cudaError_t configure() {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_adj_row<T, PLR, V, NTR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_row);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_adj_col_in<T, PLC, NTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_adj_col_out<T, PLC, NTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_col_inv<T, PLC, NTC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_col);
+    return e;
+  }
+  static void col_in(const StepArgs& a, cudaStream_t s) { k_adj_col_in<T, PLC, NTC><<<a.N / 2, NTC, smem_col, s>>>(a); }
+  static void row(const StepArgs& a, cudaStream_t s) {
+    k_adj_row<T, PLR, V, NTR><<<PLR::M / V, NTR, smem_row, s>>>(a);
+  }
+  static void col_out(const StepArgs& a, cudaStream_t s) {
+    k_adj_col_out<T, PLC, NTC><<<a.N / 2, NTC, smem_col, s>>>(a);
+  }
+  static void col_vel(const StepArgs& a, cudaStream_t s) { k_col_inv<T, PLC, NTC><<<a.N / 2, NTC, smem_col, s>>>(a); }
+  static void seed(const void* om, void* lom, void* lf, int N, double* loss_part, int blocks, cudaStream_t s) {
+    k_adj_seed<T><<<blocks, 256, 0, s>>>(static_cast<const cplx<T>*>(om), static_cast<cplx<T>*>(lom),
+                                         static_cast<cplx<T>*>(lf), N, loss_part);
+  }
+  static const AdjKernels* get() {
+    static const AdjKernels k = {PLR::TW_TOTAL,   PLC::TW_TOTAL, configure, col_in, row, col_out, col_vel,
+                                 launch_twiddles<T, PLR>, launch_twiddles<T, PLC>, seed};
+    return &k;
+  }
+};
+
 template <typename T>
 void launch_spectral(const StepArgs& a, cudaStream_t s, int blocks) {
   k_spectral<T, kSpectralThreads><<<dim3(blocks, a.members > 1 ? a.members : 1), kSpectralThreads, 0, s>>>(a);
@@ -131,7 +181,8 @@ void launch_pixels(const void* plane, long long n, double* part, unsigned int* c
   k_pixels<T><<<1024, 256, 0, s>>>(static_cast<const T*>(plane), n, mm, pix);
 }
 
-#define PAL_KERNEL_SET(T, PREC, N, ROWS, COLS)                                                          \
+#define PAL_KERNEL_SET(T, PREC, N, ROWS, COLS) PAL_KERNEL_SET_ADJ(T, PREC, N, ROWS, COLS, nullptr)
+#define PAL_KERNEL_SET_ADJ(T, PREC, N, ROWS, COLS, ADJ)                                                 \
   static const ::pal::KernelSet kSet##N = {N,                                                           \
                                            3 * (N) / 2,                                                 \
                                            PREC,                                                        \
@@ -143,7 +194,8 @@ void launch_pixels(const void* plane, long long n, double* part, unsigned int* c
                                            ::pal::launch_transpose<T>,                                  \
                                            ::pal::launch_spectrum<T>,                                   \
                                            ::pal::launch_speed<T>,                                      \
-                                           ::pal::launch_pixels<T>};
+                                           ::pal::launch_pixels<T>,                                     \
+                                           ADJ};
 
 }  // namespace pal
 

@@ -192,6 +192,14 @@ class Field:
         self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_UR_U if comp == 0 else L.PAL_FIELD_UR_V, L.ptr(a)))
         return a
 
+    def adjoint_palinstrophy(self, nsteps: int, ckpt_every: int = 20):
+        """(L, dL/d om2) for L = final palinstrophy after nsteps fixed-dt RK3 steps."""
+        g = np.empty((self.N, self.N // 2), self.cdt)
+        loss = L._D()
+        self._ck(self.lib.pal_adjoint_palinstrophy(self.h, int(nsteps), int(ckpt_every), L.ctypes.byref(loss),
+                                                   L.ptr(g)))
+        return loss.value, g
+
     def vis(self, var: int, field: bool = True, pixels: bool = False):
         """Display field var (VAR_U..VAR_STREAM): (float field or None, uint8 pixels or None)."""
         f = np.empty((self.M, self.M), self.rdt) if field else None

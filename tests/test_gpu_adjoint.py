@@ -1,0 +1,104 @@
+"""Hand-written adjoint of the RK3 step: gradient of the final palinstrophy
+with respect to the initial vorticity, against autograd through the torch.fft
+restatement and against central finite differences of the GPU forward."""
+import numpy as np
+import pytest
+
+from oracle import pao_generator as pg
+from oracle import torch_step as tsr
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ts(built_lib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from palinstrophy_gb300 import turbo_simulator
+    return turbo_simulator
+
+
+def _field(ts, N, prec, om0, dt, visc):
+    F = ts.Field(N, prec, 1.0 / visc, 0.5)
+    F.set_state(om0, None, None)
+    F.set_scalar("visc", visc)
+    F.set_scalar("dt", dt)
+    return F
+
+
+def _loss(ts, N, prec, om0, dt, visc, nsteps):
+    F = _field(ts, N, prec, om0, dt, visc)
+    F.step("LS_IMEX_RK3", nsteps, update=0)
+    om = F.om2().astype(np.complex128)
+    F.close()
+    kx = np.arange(N // 2)[None, :]
+    kz = np.fft.fftfreq(N, 1.0 / N)[:, None]
+    w = np.where(kx == 0, 1.0, 2.0)
+    return 0.5 * float((w * (kx * kx + kz * kz) * np.abs(om) ** 2).sum())
+
+
+N, DT, VISC, STEPS = 64, 2e-3, 2e-4, 12
+
+
+@pytest.fixture(scope="module")
+def start():
+    return pg.generate(N, 8.0, 5e3, 7, "PAO")["om2"].astype(np.complex128)
+
+
+@pytest.fixture(scope="module")
+def reference(start):
+    return tsr.loss_and_grad(start, N, DT, VISC, STEPS)
+
+
+def test_fp64_gradient_equals_autograd(ts, start, reference):
+    F = _field(ts, N, "fp64", start, DT, VISC)
+    L, g = F.adjoint_palinstrophy(STEPS, 4)
+    F.close()
+    L_ref, g_ref = reference
+    assert abs(L - L_ref) <= 1e-12 * L_ref
+    err = np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
+    assert err <= 1e-10, err
+
+
+def test_fp64_gradient_vs_central_differences(ts, start):
+    F = _field(ts, N, "fp64", start, DT, VISC)
+    _, g = F.adjoint_palinstrophy(STEPS, 5)
+    F.close()
+    rng = np.random.default_rng(0)
+    for _ in range(4):
+        d = rng.standard_normal(start.shape) + 1j * rng.standard_normal(start.shape)
+        eps = 1e-4 * np.linalg.norm(start) / np.linalg.norm(d)
+        lp = _loss(ts, N, "fp64", start + eps * d, DT, VISC, STEPS)
+        lm = _loss(ts, N, "fp64", start - eps * d, DT, VISC, STEPS)
+        fd = (lp - lm) / (2 * eps)
+        ad = float(np.real(np.vdot(g, d)))
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+def test_checkpoint_interval_does_not_change_gradient(ts, start):
+    gs = []
+    for ck in (1, 5, STEPS):
+        F = _field(ts, N, "fp64", start, DT, VISC)
+        gs.append(F.adjoint_palinstrophy(STEPS, ck)[1])
+        F.close()
+    for g in gs[1:]:
+        assert np.linalg.norm(g - gs[0]) / np.linalg.norm(gs[0]) <= 1e-12
+
+
+def test_fp32_gradient_within_1e4(ts, start, reference):
+    F = _field(ts, N, "fp32", start, DT, VISC)
+    L, g = F.adjoint_palinstrophy(STEPS, 4)
+    F.close()
+    L_ref, g_ref = reference
+    assert np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref) <= 1e-4
+    assert abs(L - L_ref) <= 1e-5 * L_ref
+
+
+def test_autograd_function(ts, start, reference):
+    import torch
+    from palinstrophy_gb300.autograd import PalinstrophyLoss
+    om0 = torch.as_tensor(start).clone().requires_grad_(True)
+    L = PalinstrophyLoss.apply(om0, N, "fp64", DT, VISC, STEPS, 4)
+    (2.0 * L).backward()
+    assert np.linalg.norm(om0.grad.numpy() - 2.0 * reference[1]) / np.linalg.norm(2.0 * reference[1]) <= 1e-10

@@ -241,6 +241,85 @@ def _ensemble_rate(steps=1000, warmup=20):
             "launches_per_step": 6, "cuda_graph": True, "sample_member_dt": dts}
 
 
+def _differentiation(directions=8):
+    """Gradient of the final palinstrophy after 200 fixed-dt (2e-3) LS-IMEX-RK3 steps at
+    N=512, Re=5e3, PAO K0=12 seed 7, FP32, checkpoints every 20 steps: cost of the
+    backward sweep against the forward run, and central differences (eps = 1e-3
+    relative) of the FP64 forward along 8 seeded Gaussian directions."""
+    import numpy as np
+    import torch
+    from palinstrophy_gb300 import _lib as L
+    from palinstrophy_gb300.turbo_simulator import Field
+    N, dt, Re, nsteps, ck = 512, 2e-3, 5e3, 200, 20
+    om0, _, st = L.pao_generate(N, 12.0, Re, 7, "PAO")
+    visc = st["visc"]
+
+    def field(prec):
+        F = Field(N, prec, Re, 0.5)
+        F.set_state(om0, None, None)
+        F.set_scalar("visc", visc)
+        F.set_scalar("dt", dt)
+        return F
+
+    def loss_of(om):
+        om = om.astype(np.complex128)
+        kx = np.arange(N // 2)[None, :]
+        kz = np.fft.fftfreq(N, 1.0 / N)[:, None]
+        return 0.5 * float((np.where(kx == 0, 1.0, 2.0) * (kx * kx + kz * kz) * np.abs(om) ** 2).sum())
+
+    F = field("fp32")
+    s = torch.cuda.ExternalStream(F.stream_ptr())
+    F.step("LS_IMEX_RK3", 5, update=0)
+    F.close()
+    F = field("fp32")
+    F.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s = torch.cuda.ExternalStream(F.stream_ptr())
+    e0.record(s)
+    F.step("LS_IMEX_RK3", nsteps, update=0)
+    e1.record(s)
+    e1.synchronize()
+    t_fwd = e0.elapsed_time(e1) / 1000.0
+    F.close()
+    F = field("fp32")
+    F.adjoint_palinstrophy(nsteps, ck)  # warm-up: graph capture, allocator
+    F.close()
+    F = field("fp32")
+    F.synchronize()
+    t0 = time.perf_counter()
+    loss, grad = F.adjoint_palinstrophy(nsteps, ck)
+    t_grad = time.perf_counter() - t0
+    F.close()
+    F = field("fp64")
+    _, grad64 = F.adjoint_palinstrophy(nsteps, ck)
+    F.close()
+    grad64 = grad64.astype(np.complex128)
+    rng = np.random.default_rng(12345)
+    errs, errs64 = [], []
+    for _ in range(directions):
+        d = (rng.standard_normal(om0.shape) + 1j * rng.standard_normal(om0.shape)).astype(np.complex128)
+        eps = 1e-3 * np.linalg.norm(om0) / np.linalg.norm(d)
+        vals = []
+        for sgn in (1.0, -1.0):
+            G = Field(N, "fp64", Re, 0.5)
+            G.set_state(om0.astype(np.complex128) + sgn * eps * d, None, None)
+            G.set_scalar("visc", visc)
+            G.set_scalar("dt", dt)
+            G.step("LS_IMEX_RK3", nsteps, update=0)
+            vals.append(loss_of(G.om2()))
+            G.close()
+        fd = (vals[0] - vals[1]) / (2 * eps)
+        ad = float(np.real(np.vdot(grad.astype(np.complex128), d)))
+        errs.append(abs(fd - ad) / abs(fd))
+        errs64.append(abs(fd - float(np.real(np.vdot(grad64, d)))) / abs(fd))
+    return {"N": N, "steps": nsteps, "checkpoint_every": ck, "precision": "fp32", "loss": loss,
+            "forward_s": t_fwd, "gradient_call_s": t_grad,
+            "backward_over_forward": (t_grad - t_fwd) / t_fwd,
+            "fd_directions": directions, "fd_eps_rel": 1e-3, "fd_forward": "fp64",
+            "fd_max_rel_err_fp32_adjoint": max(errs), "fd_max_rel_err_fp64_adjoint": max(errs64),
+            "grad_rel_l2_fp32_vs_fp64_adjoint": float(np.linalg.norm(grad - grad64) / np.linalg.norm(grad64))}
+
+
 def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
     """FP32 CPU port of the reference path: steps/s over a bounded sample."""
     import numpy as np
@@ -332,6 +411,7 @@ def run_gb300(args):
 
     e2e_rate, h2d, d2h = _e2e("fp32", om2, uc, visc, args.steps)
     ens = _ensemble_rate()
+    diff = _differentiation()
 
     rate32 = ws * args.steps / (ms32 / 1000.0)
     rate64 = ws * k64 / (ms64 / 1000.0)
@@ -372,6 +452,7 @@ def run_gb300(args):
                      "ms_per_launch": {"k_row": ms_row, "k_col": ms_col},
                      "stage_bytes_per_s": (bytes_row + bytes_col) / ((ms_row + ms_col) / 1000.0) / 1e9},
         "ensemble": ens,
+        "differentiation": diff,
         "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": min(8, os.cpu_count() or 1),
                          "kind": "port",
                          "sample": f"{cpu_n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up ({cpu_s:.1f} s), FP32 "

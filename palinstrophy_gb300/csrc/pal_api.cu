@@ -651,36 +651,26 @@ int pal_adjoint_palinstrophy(pal_handle* h, int nsteps, int ckpt_every, double* 
   adj->tw_col(tw_c, h->stream);
   int rc = PAL_OK;
   auto seg_len = [&](int seg) { return std::min(ckpt_every, nsteps - seg * ckpt_every); };
-  // forward sweep with checkpoints (fixed dt: no NEXTDT)
-  for (int seg = 0; seg < n_ck && rc == PAL_OK; ++seg) {
-    cudaMemcpyAsync(ck + 2 * plane_om * seg, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-    cudaMemcpyAsync(ck + 2 * plane_om * seg + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-    for (int j = 0; j < seg_len(seg) && rc == PAL_OK; ++j) rc = one_step(h, PAL_LS_IMEX_RK3, false, true);
-  }
-  if (rc) {
-    cudaFreeAsync(buf, h->stream);
-    return rc;
-  }
-  cudaMemcpyAsync(fin, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-  cudaMemcpyAsync(fin + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-  adj->seed(h->om, lom, lf, h->N, loss_part, seed_blocks, h->stream);
-  // backward sweep: per segment, recompute and store the stage inputs, then run
-  // the adjoint stages in reverse
-  for (int seg = n_ck - 1; seg >= 0 && rc == PAL_OK; --seg) {
-    cudaMemcpyAsync(h->om, ck + 2 * plane_om * seg, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-    cudaMemcpyAsync(h->fnm1, ck + 2 * plane_om * seg + plane_om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+  // Segments are launch sequences with fixed buffers; full-length segments are
+  // captured once as CUDA graphs (forward, and recompute + adjoint sweep) and
+  // replayed, the checkpoint copies staying outside the graphs.
+  auto forward_body = [&](int ns) -> int {
+    int r = PAL_OK;
+    for (int j = 0; j < ns && r == PAL_OK; ++j) r = one_step(h, PAL_LS_IMEX_RK3, false, true);
+    return r;
+  };
+  auto backward_body = [&](int ns) -> int {
     h->state = ST_VEL_PENDING;
     h->vel_uploaded = false;
-    if ((rc = resolve_velocity(h))) break;
-    const int ns = seg_len(seg);
-    for (int j = 0; j < ns && rc == PAL_OK; ++j) {
-      for (int s = 0; s < 3 && rc == PAL_OK; ++s) {
+    int r = resolve_velocity(h);
+    for (int j = 0; j < ns && r == PAL_OK; ++j) {
+      for (int s = 0; s < 3 && r == PAL_OK; ++s) {
         cudaMemcpyAsync(st + plane_om * (size_t)(3 * j + s), h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
-        if ((rc = launch_row(h, 0))) break;
-        rc = launch_col(h, 1, s, 0);
+        if ((r = launch_row(h, 0))) break;
+        r = launch_col(h, 1, s, 0);
       }
     }
-    for (int q = 3 * ns - 1; q >= 0 && rc == PAL_OK; --q) {
+    for (int q = 3 * ns - 1; q >= 0 && r == PAL_OK; --q) {
       const int s = q % 3;
       StepArgs a = base_args(h);
       a.om = lom;
@@ -703,9 +693,57 @@ int pal_adjoint_palinstrophy(pal_handle* h, int nsteps, int ckpt_every, double* 
       a.tw = tw_c;
       adj->col_out(a, h->stream);
       cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) rc = cuda_fail(h, e, "adjoint stage");
+      if (e != cudaSuccess) r = cuda_fail(h, e, "adjoint stage");
+    }
+    return r;
+  };
+  auto capture = [&](auto&& body, int ns, cudaGraphExec_t* exec) -> int {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
+    const int r = body(ns);
+    e = cudaStreamEndCapture(h->stream, &g);
+    if (r) return r;
+    if (e != cudaSuccess) return cuda_fail(h, e, "end capture");
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph instantiate");
+    return PAL_OK;
+  };
+  const bool use_graphs = !(std::getenv("PAL_ADJOINT_GRAPHS") && std::getenv("PAL_ADJOINT_GRAPHS")[0] == '0');
+  cudaGraphExec_t g_fwd = nullptr, g_bwd = nullptr;
+  // forward sweep with checkpoints (fixed dt: no NEXTDT)
+  for (int seg = 0; seg < n_ck && rc == PAL_OK; ++seg) {
+    cudaMemcpyAsync(ck + 2 * plane_om * seg, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(ck + 2 * plane_om * seg + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    const int ns = seg_len(seg);
+    if (use_graphs && ns == ckpt_every) {
+      if (!g_fwd) rc = capture(forward_body, ns, &g_fwd);
+      if (rc == PAL_OK && cudaGraphLaunch(g_fwd, h->stream) != cudaSuccess) rc = fail(h, PAL_ERR_CUDA, "graph launch");
+    } else {
+      rc = forward_body(ns);
     }
   }
+  if (rc == PAL_OK) {
+    cudaMemcpyAsync(fin, h->om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(fin + plane_om, h->fnm1, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    adj->seed(h->om, lom, lf, h->N, loss_part, seed_blocks, h->stream);
+  }
+  // backward sweep: per segment, recompute and store the stage inputs, then run
+  // the adjoint stages in reverse
+  for (int seg = n_ck - 1; seg >= 0 && rc == PAL_OK; --seg) {
+    cudaMemcpyAsync(h->om, ck + 2 * plane_om * seg, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(h->fnm1, ck + 2 * plane_om * seg + plane_om, plane_om, cudaMemcpyDeviceToDevice, h->stream);
+    const int ns = seg_len(seg);
+    if (use_graphs && ns == ckpt_every) {
+      if (!g_bwd) rc = capture(backward_body, ns, &g_bwd);
+      if (rc == PAL_OK && cudaGraphLaunch(g_bwd, h->stream) != cudaSuccess) rc = fail(h, PAL_ERR_CUDA, "graph launch");
+    } else {
+      rc = backward_body(ns);
+    }
+  }
+  if (g_fwd) cudaGraphExecDestroy(g_fwd);
+  if (g_bwd) cudaGraphExecDestroy(g_bwd);
   // leave the handle at the final forward state
   cudaMemcpyAsync(h->om, fin, plane_om, cudaMemcpyDeviceToDevice, h->stream);
   cudaMemcpyAsync(h->fnm1, fin + plane_om, plane_om, cudaMemcpyDeviceToDevice, h->stream);

@@ -133,6 +133,12 @@ def check(rc, h=None):
     return rc
 
 
+def supported(N, precision="fp32") -> bool:
+    """True if kernels for this grid size and precision are compiled in."""
+    prec = {"fp32": PAL_FP32, "fp64": PAL_FP64}[precision]
+    return load().pal_supported(int(N), prec) == 1
+
+
 def ptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.c_void_p)
 

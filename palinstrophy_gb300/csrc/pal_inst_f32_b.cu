@@ -18,21 +18,23 @@ const RowKernels r1024[] = {RowOf<float, P1536, 4, 256>::make("16.4.24 V4x256"),
                             RowOf<float, P1536b, 4, 256>::make("8.8.24 V4x256")};
 const ColKernels c1024[] = {ColOf<float, P1536, 256>::make("16.4.24 x256"), ColOf<float, P1536, 128>::make("16.4.24 x128"),
                             ColOf<float, P1536b, 256>::make("8.8.24 x256"),
-                            ColOf<float, Rec<P1536>, 128, true>::make("16.4.24r x128 pref"),
-                            ColOf<float, Rec<P1536>, 256, true>::make("16.4.24r x256 pref")};
+                            ColOf<float, Rec<P1536>, 128, 1>::make("16.4.24r x128 pref"),
+                            ColOf<float, Rec<P1536>, 256, 1>::make("16.4.24r x256 pref")};
 const RowKernels r1536[] = {RowOf<float, P2304, 4, 512>::make("16.6.24 V4x512"),
                             RowOf<float, P2304, 2, 256>::make("16.6.24 V2x256")};
 const ColKernels c1536[] = {ColOf<float, P2304, 256>::make("16.6.24 x256"), ColOf<float, P2304, 128>::make("16.6.24 x128")};
 const RowKernels r2048[] = {RowOf<float, P3072, 4, 512>::make("16.8.24 V4x512"),
                             RowOf<float, Rec<P3072>, 4, 512>::make("16.8.24r V4x512"),
+                            RowOf<float, Rec<P3072>, 4, 512, 1>::make("16.8.24r V4x512 l2pf"),
                             RowOf<float, P3072, 2, 256>::make("16.8.24 V2x256"),
                             RowOf<float, P3072, 1, 256>::make("16.8.24 V1x256"),
                             RowOf<float, P3072b, 2, 256>::make("8.16.24 V2x256")};
 const ColKernels c2048[] = {ColOf<float, P3072, 256>::make("16.8.24 x256"), ColOf<float, P3072, 512>::make("16.8.24 x512"),
                             ColOf<float, P3072b, 256>::make("8.16.24 x256"),
                             ColOf<float, Rec<P3072b>, 256>::make("8.16.24r x256"),
-                            ColOf<float, Rec<P3072b>, 256, true>::make("8.16.24r x256 pref"),
-                            ColOf<float, Rec<P3072b>, 512, true>::make("8.16.24r x512 pref")};
+                            ColOf<float, Rec<P3072b>, 256, 1>::make("8.16.24r x256 pref"),
+                            ColOf<float, Rec<P3072b>, 512, 1>::make("8.16.24r x512 pref"),
+                            ColOf<float, Rec<P3072b>, 256, 2>::make("8.16.24r x256 l2pf")};
 const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512"),
                             RowOf<float, P4608, 2, 256>::make("16.12.24 V2x256")};
 const ColKernels c3072[] = {ColOf<float, P4608, 256>::make("16.12.24 x256"), ColOf<float, P4608, 512>::make("16.12.24 x512")};

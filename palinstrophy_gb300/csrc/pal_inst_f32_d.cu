@@ -5,15 +5,13 @@ using namespace pal;
 
 namespace {
 using P12288 = Plan<12288, 16, 32, 24>;
-using P12288b = Plan<12288, 32, 16, 24>;
 
 const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"),
-                            RowOf<float, Rec<P12288>, 2, 256>::make("16.32.24r V2x256"),
                             RowOf<float, Rec<P12288>, 2, 512>::make("16.32.24r V2x512"),
-                            RowOf<float, P12288, 1, 256>::make("16.32.24 V1x256"),
-                            RowOf<float, P12288b, 2, 256>::make("32.16.24 V2x256")};
-const ColKernels c8192[] = {ColOf<float, P12288, 256>::make("16.32.24 x256"), ColOf<float, P12288, 512>::make("16.32.24 x512"),
-                            ColOf<float, P12288b, 256>::make("32.16.24 x256"),
+                            RowOf<float, Rec<P12288>, 2, 512, 1>::make("16.32.24r V2x512 l2pf"),
+                            RowOf<float, Rec<P12288>, 2, 512, 2>::make("16.32.24r V2x512 paired"),
+                            RowOf<float, Rec<P12288>, 2, 512, 3>::make("16.32.24r V2x512 paired l2pf")};
+const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512")};
 
 PAL_KERNEL_SET(float, 0, 8192, r8192, c8192)

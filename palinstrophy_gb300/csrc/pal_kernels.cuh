@@ -64,6 +64,7 @@ struct StepArgs {
   long long ms_w, ms_om, ms_part, ms_phys, ms_src;
   const void* y0;   // adjoint: the forward velocity planes of the stage
   const void* y1;
+  int ahead;        // resident blocks of one wave (L2-prefetch candidates; 0 = none)
 };
 
 // Member view of the arguments for block row blockIdx.y.
@@ -227,6 +228,78 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
   __syncthreads();
 }
 
+// First inverse DIF pass with each U-state row read once.  Butterfly i holds
+// z[i + j S]; the mirrored entry z[M - k] = conj(u^[k]) + i conj(v^[k]) of a
+// row k = i + j S < N/2 sits in butterfly S - i at index R-1-j (for i = 0: in
+// butterfly 0 at (R-j) mod R).  One thread loads the rows below N/2 of the pair
+// (i, S - i) and fills both butterflies, halving the global loads of the pass.
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>* sm, int z0, int tid) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  constexpr int SP = PL::pstride(0);
+  constexpr int Nh = M / 3;
+  constexpr int NQ = S / 2 + 1;
+  static_assert(S % 2 == 0, "paired first pass needs an even stride");
+  const C* __restrict__ w0 = static_cast<const C*>(a.w0);
+  const C* __restrict__ w1 = static_cast<const C*>(a.w1);
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  for (int w = tid; w < V * NQ; w += NT) {
+    const int v = w % V;
+    const int q = w / V;
+    const bool two = q > 0 && 2 * q < S;
+    const int i2 = S - q;
+    const size_t col = (size_t)z0 + v;
+    C x[R], y[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = y[j] = C{T(0), T(0)};
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (j * S >= Nh) continue;  // folded at compile time
+      const int k1 = q + j * S;
+      if (j * S + S - 1 < Nh || k1 < Nh) {
+        const C u = w0[(size_t)k1 * M + col], qv = w1[(size_t)k1 * M + col];
+        const C m = C{u.x + qv.y, qv.x - u.y};
+        if (q == 0) {
+          if (j == 0) {
+            x[0] = C{u.x, qv.x};
+          } else {
+            x[j] = C{u.x - qv.y, u.y + qv.x};
+            x[(R - j) % R] = m;
+          }
+        } else {
+          x[j] = C{u.x - qv.y, u.y + qv.x};
+          if (two) y[R - 1 - j] = m;
+          else x[R - 1 - j] = m;
+        }
+      }
+      const int k2 = i2 + j * S;
+      if (two && (j * S + S - 1 < Nh || k2 < Nh)) {
+        const C u = w0[(size_t)k2 * M + col], qv = w1[(size_t)k2 * M + col];
+        y[j] = C{u.x - qv.y, u.y + qv.x};
+        x[R - 1 - j] = C{u.x + qv.y, qv.x - u.y};
+      }
+    }
+    Dft<R, +1, C>::run(x);
+    pass_tw<PL, 0, +1>(x, tw, q);
+    {
+      C* p = sm + PL::phys(q) * V + v;
+#pragma unroll
+      for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
+    }
+    if (two) {
+      Dft<R, +1, C>::run(y);
+      pass_tw<PL, 0, +1>(y, tw, i2);
+      C* p = sm + PL::phys(i2) * V + v;
+#pragma unroll
+      for (int k = 0; k < R; ++k) p[k * SP * V] = y[k];
+    }
+  }
+  __syncthreads();
+}
+
 // Last forward DIT pass of the row kernel fused with the Hermitian unpack.
 // Butterfly i produces P[i + j S]; the conjugate partner P[M - i - j S] sits in
 // butterfly S - i at index R-1-j (or, for i = 0, in butterfly 0 at (R-j) mod R),
@@ -291,8 +364,21 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
   }
 }
 
+// L2 prefetch helpers.  `cp.async.bulk.prefetch.L2` pulls a contiguous,
+// 16-byte aligned range into L2 without occupying registers or the LSU queue;
+// `prefetch.global.L2` does one line.  Both are hints with no visible effect.
+__device__ __forceinline__ void l2_prefetch_bulk(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void l2_prefetch_line(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // k_row: U-state rows -> P-state rows (products), optional CFL statistics.
-template <typename T, class PL, int V, int NT>
+// PF bit 0: the tile one wave ahead (blockIdx.x + a.ahead) is pulled into L2
+// first, so that the block that will run it finds its rows there.
+// PF bit 1: the first pass reads every U-state row once (row_first_pass_paired).
+template <typename T, class PL, int V, int NT, int PF>
 __global__ void __launch_bounds__(NT) k_row(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
@@ -303,7 +389,20 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a0) {
   const int z0 = blockIdx.x * V;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
 
-  row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
+  if constexpr ((PF & 1) != 0) {
+    const int nb = (int)blockIdx.x + a.ahead;
+    if (a.ahead > 0 && nb < (int)gridDim.x) {
+      constexpr int Nh = M / 3;
+      const cplx<T>* w0 = static_cast<const cplx<T>*>(a.w0) + (size_t)nb * V;
+      const cplx<T>* w1 = static_cast<const cplx<T>*>(a.w1) + (size_t)nb * V;
+      for (int r = tid; r < 2 * Nh; r += NT) l2_prefetch_line((r < Nh ? w0 : w1) + (size_t)(r < Nh ? r : r - Nh) * M);
+    }
+  }
+  if constexpr ((PF & 2) != 0) {
+    row_first_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
+  } else {
+    row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
+  }
   dif_range<T, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
 
   // middle: last inverse DIF pass -> products -> first forward DIT pass
@@ -414,10 +513,172 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF the
-// column's om and fnm1 are copied into shared memory asynchronously at entry,
-// so the update reads them without exposed global latency.
-template <typename T, class PL, int NT, bool PREF>
+// Implicit / explicit weights of the column update, formed in FP64 from the
+// device scalars: CNAB2 (turbo_simulator.py:1745-1752) or one RK3 stage.
+template <typename T>
+__device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
+  ModeCoef<T> cf;
+  const DevScalars* sc = a.sc;
+  const double dt = sc->dt, visc = sc->visc;
+  double h1, h2, c2, c3;
+  if (a.scheme == 0) {
+    const double cnm1 = sc->cnm1;
+    h1 = h2 = (0.5 * visc) * dt;
+    c2 = (0.5 * dt) * (2.0 + cnm1);
+    c3 = (-0.5 * dt) * cnm1;
+  } else {
+    h1 = (a.beta * dt) * visc;
+    h2 = (a.alpha * dt) * visc;
+    c2 = a.alpha * dt;
+    c3 = a.beta * dt;
+  }
+  cf.h1 = T(h1);
+  cf.h2 = T(h2);
+  cf.c2 = T(c2);
+  cf.c3 = T(c3);
+  const T m32 = T(1.5) * T(N);
+  cf.divxz = T(1) / (m32 * m32);
+  return cf;
+}
+
+// Middle of the column pass: last forward DIF -> nonlinear term, update,
+// inversion -> first inverse DIT.  The two lanes of a butterfly hold A and B;
+// lane 0 updates the even positions and lane 1 the odd ones, trading operands
+// and results by shuffle.  When 3 divides the radix, the de-aliased band
+// (frequencies N/2 .. N-1, the middle third of the positions) is known at
+// compile time and skipped.  om / fm are read from s_om / s_fm when SMEM_OM.
+template <typename T, class PL, int NT, bool SMEM_OM>
+__device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
+                                           cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
+                                           const ModeCoef<T>& cf, int kx, int tid) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int V = 2;
+  constexpr int N = 2 * M / 3, Nh = M / 3;
+  constexpr int R = PL::RP;
+  constexpr int NB = V * (M / R);
+  constexpr int FSTEP = M / R;
+  constexpr bool BAND_CT = (R % 3 == 0) && ((R / 3) % 2 == 0);
+  const T ax = T(kx);
+  for (int w0i = 0; w0i < NB; w0i += NT) {
+    const int w = w0i + tid;
+    const bool act = w < NB;
+    const int v = w & 1;
+    const int b = act ? (w >> 1) : 0;
+    C* p = sm + b * (R + 1) * V + v;
+    const int fb = PL::freq(b * R);
+    C x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = act ? p[j * V] : C{T(0), T(0)};
+    Dft<R, -1, C>::run(x);
+#pragma unroll
+    for (int j = 0; j < R; j += 2) {
+      if (BAND_CT && j >= R / 3 && j < 2 * R / 3) {
+        x[j] = C{T(0), T(0)};
+        x[j + 1] = C{T(0), T(0)};
+        continue;
+      }
+      // lane 0 takes position j, lane 1 position j+1
+      const C send = v == 0 ? x[j + 1] : x[j];
+      C recv;
+      recv.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
+      recv.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+      const C Az = v == 0 ? x[j] : recv;
+      const C Bz = v == 0 ? recv : x[j + 1];
+      const int f = fb + (j + v) * FSTEP;
+      const bool inband = act && (BAND_CT || f < Nh || f >= N);
+      const int z = f < Nh ? f : f - Nh;
+      C uh = {T(0), T(0)}, vh = {T(0), T(0)};
+      if (inband) {
+        const C o = SMEM_OM ? s_om[z] : om[z];
+        const C fo = SMEM_OM ? s_fm[z] : fm[z];
+        const T gz = T(z < Nh ? z : z - N);
+        const T K2 = ax * ax + gz * gz;
+        const T GA = gz * ax;
+        const T G2mA2 = gz * gz - ax * ax;
+        C fn = {T(0), T(0)};
+        if (z != Nh) {
+          fn.x = (Az.x * GA + Bz.x * G2mA2) * cf.divxz;
+          fn.y = (Az.y * GA + Bz.y * G2mA2) * cf.divxz;
+        }
+        const T c1 = T(1) - K2 * cf.h1;
+        const T rden = T(1) / (T(1) + K2 * cf.h2);
+        C on;
+        on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
+        on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
+        om[z] = on;
+        fm[z] = fn;
+        if (kx >= 1) {
+          const T ik = T(1) / K2;
+          const C t = {on.x * ik, on.y * ik};
+          uh = C{t.y * gz, -t.x * gz};
+          vh = C{-t.y * ax, t.x * ax};
+        } else if (z >= 1) {
+          const T ig = T(1) / gz;
+          uh = C{on.y * ig, -on.x * ig};
+        }
+      }
+      // lane 0 keeps u^ of position j and receives u^ of j+1; lane 1 the v^ pair
+      const C send2 = v == 0 ? vh : uh;
+      C recv2;
+      recv2.x = __shfl_xor_sync(0xffffffffu, send2.x, 1);
+      recv2.y = __shfl_xor_sync(0xffffffffu, send2.y, 1);
+      x[j] = v == 0 ? uh : recv2;
+      x[j + 1] = v == 0 ? recv2 : vh;
+    }
+    Dft<R, +1, C>::run(x);
+    if (act) {
+#pragma unroll
+      for (int j = 0; j < R; ++j) p[j * V] = x[j];
+    }
+  }
+  __syncthreads();
+}
+
+// Last inverse DIT pass of the column straight into the U planes.
+template <typename T, class PL, int NT>
+__device__ __forceinline__ void col_last_pass(const cplx<T>* sm, cplx<T>* __restrict__ w0, cplx<T>* __restrict__ w1,
+                                              const cplx<T>* __restrict__ tw, int kx, int tid) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int V = 2;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  for (int w = tid; w < V * S; w += NT) {
+    const int v = w & 1;
+    const int i = w >> 1;
+    C* __restrict__ dst = (v == 0 ? w0 : w1) + (size_t)kx * M;
+    const C* p = sm + PL::phys(i) * V + v;
+    C x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = p[k * PL::pstride(0) * V];
+    pass_tw<PL, 0, +1>(x, tw, i);
+    Dft<R, +1, C>::run(x);
+#pragma unroll
+    for (int j = 0; j < R; ++j) dst[i + j * S] = x[j];
+  }
+}
+
+// Time / cnm1 bookkeeping of the step, done once by the last block to finish.
+template <int NT>
+__device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
+  if (a.flags & (F_ADVANCE | F_CNM1)) {
+    if (last_block(&a.sc->col_counter, tid) && tid == 0) {
+      DevScalars* sc = a.sc;
+      if (a.flags & F_ADVANCE) {
+        sc->t += sc->dt;
+        sc->it += 1;
+      }
+      if (a.flags & F_CNM1) sc->cnm1 = sc->cn;
+      sc->col_counter = 0u;
+    }
+  }
+}
+
+// k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF == 1
+// the column's om and fnm1 are copied into shared memory asynchronously at
+// entry, so the update reads them without exposed global latency.
+template <typename T, class PL, int NT, int PREF>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
@@ -427,7 +688,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   constexpr int V = 2;
   const int tid = threadIdx.x;
   const int kx = blockIdx.x;
-  constexpr int N = 2 * M / 3, Nh = M / 3;
+  constexpr int N = 2 * M / 3;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   C* __restrict__ w0 = static_cast<C*>(a.w0);
   C* __restrict__ w1 = static_cast<C*>(a.w1);
@@ -435,7 +696,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   C* __restrict__ fm = static_cast<C*>(a.fnm1) + (size_t)kx * N;
   C* s_om = sm + PL::PADM * V;
   C* s_fm = s_om + N;
-  if constexpr (PREF) {
+  if constexpr (PREF == 1) {
     constexpr int CH = N * (int)sizeof(C) / 16;
     for (int c = tid; c < 2 * CH; c += NT) {
       const bool second = c >= CH;
@@ -445,31 +706,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     }
     cp_async_commit();
   }
-
-  // implicit / explicit weights, formed in FP64 from the device scalars
-  ModeCoef<T> cf;
-  {
-    const DevScalars* sc = a.sc;
-    const double dt = sc->dt, visc = sc->visc;
-    double h1, h2, c2, c3;
-    if (a.scheme == 0) {
-      const double cnm1 = sc->cnm1;
-      h1 = h2 = (0.5 * visc) * dt;
-      c2 = (0.5 * dt) * (2.0 + cnm1);
-      c3 = (-0.5 * dt) * cnm1;
-    } else {
-      h1 = (a.beta * dt) * visc;
-      h2 = (a.alpha * dt) * visc;
-      c2 = a.alpha * dt;
-      c3 = a.beta * dt;
-    }
-    cf.h1 = T(h1);
-    cf.h2 = T(h2);
-    cf.c2 = T(c2);
-    cf.c3 = T(c3);
-    const T m32 = T(1.5) * T(N);
-    cf.divxz = T(1) / (m32 * m32);
-  }
+  const ModeCoef<T> cf = col_coef<T>(a, N);
 
   // pass 0 (forward z-DIF) straight from the P planes
   {
@@ -491,127 +728,14 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     __syncthreads();
   }
   dif_range<T, PL, V, NT, -1, 1, PL::NP - 1>(sm, tw, tid);
-  if constexpr (PREF) {
+  if constexpr (PREF == 1) {
     cp_async_wait_all();
     __syncthreads();
   }
-
-  // middle: last forward DIF -> nonlinear term, update, inversion -> first inverse DIT.
-  // The two lanes of a butterfly hold A and B; lane 0 updates the even
-  // positions and lane 1 the odd ones, trading operands and results by shuffle.
-  // When 3 divides the radix, the de-aliased band (frequencies N/2 .. N-1, the
-  // middle third of the positions) is known at compile time and skipped.
-  {
-    constexpr int R = PL::RP;
-    constexpr int NB = V * (M / R);
-    constexpr int FSTEP = M / R;
-    constexpr bool BAND_CT = (R % 3 == 0) && ((R / 3) % 2 == 0);
-    const T ax = T(kx);
-    for (int w0i = 0; w0i < NB; w0i += NT) {
-      const int w = w0i + tid;
-      const bool act = w < NB;
-      const int v = w & 1;
-      const int b = act ? (w >> 1) : 0;
-      C* p = sm + b * (R + 1) * V + v;
-      C x[R];
-#pragma unroll
-      for (int j = 0; j < R; ++j) x[j] = act ? p[j * V] : C{T(0), T(0)};
-      Dft<R, -1, C>::run(x);
-      const int fb = PL::freq(b * R);
-#pragma unroll
-      for (int j = 0; j < R; j += 2) {
-        if (BAND_CT && j >= R / 3 && j < 2 * R / 3) {
-          x[j] = C{T(0), T(0)};
-          x[j + 1] = C{T(0), T(0)};
-          continue;
-        }
-        // lane 0 takes position j, lane 1 position j+1
-        const C send = v == 0 ? x[j + 1] : x[j];
-        C recv;
-        recv.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
-        recv.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
-        const C Az = v == 0 ? x[j] : recv;
-        const C Bz = v == 0 ? recv : x[j + 1];
-        const int f = fb + (j + v) * FSTEP;
-        const bool inband = act && (BAND_CT || f < Nh || f >= N);
-        const int z = f < Nh ? f : f - Nh;
-        C uh = {T(0), T(0)}, vh = {T(0), T(0)};
-        if (inband) {
-          const C o = PREF ? s_om[z] : om[z];
-          const C fo = PREF ? s_fm[z] : fm[z];
-          const T gz = T(z < Nh ? z : z - N);
-          const T K2 = ax * ax + gz * gz;
-          const T GA = gz * ax;
-          const T G2mA2 = gz * gz - ax * ax;
-          C fn = {T(0), T(0)};
-          if (z != Nh) {
-            fn.x = (Az.x * GA + Bz.x * G2mA2) * cf.divxz;
-            fn.y = (Az.y * GA + Bz.y * G2mA2) * cf.divxz;
-          }
-          const T c1 = T(1) - K2 * cf.h1;
-          const T rden = T(1) / (T(1) + K2 * cf.h2);
-          C on;
-          on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
-          on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
-          om[z] = on;
-          fm[z] = fn;
-          if (kx >= 1) {
-            const T ik = T(1) / K2;
-            const C t = {on.x * ik, on.y * ik};
-            uh = C{t.y * gz, -t.x * gz};
-            vh = C{-t.y * ax, t.x * ax};
-          } else if (z >= 1) {
-            const T ig = T(1) / gz;
-            uh = C{on.y * ig, -on.x * ig};
-          }
-        }
-        // lane 0 keeps u^ of position j and receives u^ of j+1; lane 1 the v^ pair
-        const C send2 = v == 0 ? vh : uh;
-        C recv2;
-        recv2.x = __shfl_xor_sync(0xffffffffu, send2.x, 1);
-        recv2.y = __shfl_xor_sync(0xffffffffu, send2.y, 1);
-        x[j] = v == 0 ? uh : recv2;
-        x[j + 1] = v == 0 ? recv2 : vh;
-      }
-      Dft<R, +1, C>::run(x);
-      if (act) {
-#pragma unroll
-        for (int j = 0; j < R; ++j) p[j * V] = x[j];
-      }
-    }
-    __syncthreads();
-  }
+  col_middle<T, PL, NT, PREF == 1>(sm, s_om, s_fm, om, fm, cf, kx, tid);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
-
-  // last inverse DIT pass straight into the U planes
-  {
-    constexpr int R = PL::R[0];
-    constexpr int S = M / R;
-    for (int w = tid; w < V * S; w += NT) {
-      const int v = w & 1;
-      const int i = w >> 1;
-      C* __restrict__ dst = (v == 0 ? w0 : w1) + (size_t)kx * M;
-      const C* p = sm + PL::phys(i) * V + v;
-      C x[R];
-#pragma unroll
-      for (int k = 0; k < R; ++k) x[k] = p[k * PL::pstride(0) * V];
-      pass_tw<PL, 0, +1>(x, tw, i);
-      Dft<R, +1, C>::run(x);
-#pragma unroll
-      for (int j = 0; j < R; ++j) dst[i + j * S] = x[j];
-    }
-  }
-  if (a.flags & (F_ADVANCE | F_CNM1)) {
-    if (last_block(&a.sc->col_counter, tid) && tid == 0) {
-      DevScalars* sc = a.sc;
-      if (a.flags & F_ADVANCE) {
-        sc->t += sc->dt;
-        sc->it += 1;
-      }
-      if (a.flags & F_CNM1) sc->cnm1 = sc->cn;
-      sc->col_counter = 0u;
-    }
-  }
+  col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
+  col_finish<NT>(a, tid);
 }
 
 // k_col_inv: velocity low band -> pad -> inverse z-FFT -> U planes.  The low

@@ -72,18 +72,33 @@ void launch_twiddles(void* tw, cudaStream_t s) {
   k_twiddles<T, PL><<<(PL::TW_TOTAL + 255) / 256, 256, 0, s>>>(static_cast<cplx<T>*>(tw));
 }
 
-template <typename T, class PL, int V, int NT>
+// Blocks of one kernel resident on the whole device at once (one wave).
+template <class K>
+inline int wave_blocks(K kernel, int nt, size_t smem) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem) != cudaSuccess) return 0;
+  return sms * per_sm;
+}
+
+template <typename T, class PL, int V, int NT, int PF = 0>
 struct RowOf {
   static constexpr size_t smem = size_t(PL::PADM) * V * sizeof(cplx<T>);
   static_assert(smem <= kSmemLimit, "row tile does not fit in shared memory");
   static_assert(PL::M % V == 0, "row tile must divide M");
+  static inline int ahead = 0;
   static cudaError_t configure() {
-    cudaError_t e = cudaFuncSetAttribute(k_row<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (PF & 1) ahead = wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   static void row(const StepArgs& a, cudaStream_t s) {
-    k_row<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
+    StepArgs b = a;
+    b.ahead = ahead;
+    k_row<T, PL, V, NT, PF><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(b);
   }
   static void phys(const StepArgs& a, cudaStream_t s) {
     k_phys<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
@@ -93,19 +108,23 @@ struct RowOf {
   }
 };
 
-template <typename T, class PL, int NT, bool PREF = false>
+template <typename T, class PL, int NT, int PREF = 0>
 struct ColOf {
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
-  static constexpr size_t smem = smem_inv + (PREF ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
+  static constexpr size_t smem = smem_inv + (PREF == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
+  static inline int ahead = 0;
   static cudaError_t configure() {
     cudaError_t e =
         cudaFuncSetAttribute(k_col<T, PL, NT, PREF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if (PREF == 2) ahead = wave_blocks(k_col<T, PL, NT, PREF>, NT, smem);
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
   static void col(const StepArgs& a, cudaStream_t s) {
-    k_col<T, PL, NT, PREF><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
+    StepArgs b = a;
+    b.ahead = ahead;
+    k_col<T, PL, NT, PREF><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem, s>>>(b);
   }
   static void col_inv(const StepArgs& a, cudaStream_t s) {
     k_col_inv<T, PL, NT><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem_inv, s>>>(a);

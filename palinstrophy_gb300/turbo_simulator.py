@@ -246,6 +246,7 @@ class DnsState:
         self.start_spectrum = start_spectrum
         self.seed_init = int(seed)
         self.populate_compact_ur = populate_compact_ur
+        self.uc_init = None  # initial velocity low band (2, N, N/2), kept for `uc`
         self.fft_workers = 1
         self.inv_dx = float(N) / (2.0 * math.pi)
         self.t = 0.0
@@ -303,6 +304,14 @@ class DnsState:
         out[:, :, 1] = full[1, off:off + n, off:off + n]
         return out
 
+    @property
+    def uc(self):
+        """Compact velocity spectrum (N, 3N/4+1, 3) as the reference keeps it: the
+        generator's initial velocity, never updated by stepping (turbo_simulator.py:944, 1221)."""
+        from .restart import uc_from_low_band
+        low = self.uc_init if self.uc_init is not None else np.zeros((2, self.NZ, self.NX // 2), np.complex64)
+        return uc_from_low_band(low, self.NZ)
+
     def set_spectral_state(self, om2, fnm1=None, uc_low=None):
         """Load om2/fnm1 (and optionally the velocity low band) from host arrays."""
         self._field.set_state(om2, fnm1, uc_low)
@@ -334,6 +343,7 @@ def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float 
     print(f" PAO seed in = {seed}")
     print(f" PAO seed out= {st['seed_out']}")
     S.set_spectral_state(om2, None, uc)
+    S.uc_init = np.asarray(uc, np.complex64)
     S.visc = float(st["visc"])
     S.dt, S.cn, S.cnm1 = 0.0, 1.0, 0.0
     return S

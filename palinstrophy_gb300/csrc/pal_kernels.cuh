@@ -230,9 +230,12 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
 
 // First inverse DIF pass with each U-state row read once.  Butterfly i holds
 // z[i + j S]; the mirrored entry z[M - k] = conj(u^[k]) + i conj(v^[k]) of a
-// row k = i + j S < N/2 sits in butterfly S - i at index R-1-j (for i = 0: in
-// butterfly 0 at (R-j) mod R).  One thread loads the rows below N/2 of the pair
-// (i, S - i) and fills both butterflies, halving the global loads of the pass.
+// row k = i + j S < N/2 sits in butterfly S - i at index R-1-j.  Butterflies 0
+// and S/2 are their own partners (at index (R-j) mod R and R-1-j).  Work item
+// q < S/2 takes the pair (q, S - q), item 0 the two self-paired butterflies
+// (0, S/2), so every item is two DFTs, V S / 2 items in all, and every row
+// below N/2 is loaded by exactly one thread: half the global loads of an
+// unpaired first pass.
 template <typename T, class PL, int V, int NT>
 __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>* sm, int z0, int tid) {
   using C = cplx<T>;
@@ -241,16 +244,16 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
   constexpr int S = M / R;
   constexpr int SP = PL::pstride(0);
   constexpr int Nh = M / 3;
-  constexpr int NQ = S / 2 + 1;
-  static_assert(S % 2 == 0, "paired first pass needs an even stride");
+  constexpr int NQ = S / 2;
+  static_assert(S % 2 == 0 && R % 2 == 0, "paired first pass needs an even stride and radix");
   const C* __restrict__ w0 = static_cast<const C*>(a.w0);
   const C* __restrict__ w1 = static_cast<const C*>(a.w1);
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   for (int w = tid; w < V * NQ; w += NT) {
     const int v = w % V;
     const int q = w / V;
-    const bool two = q > 0 && 2 * q < S;
-    const int i2 = S - q;
+    const bool self = q == 0;
+    const int i2 = self ? S / 2 : S - q;
     const size_t col = (size_t)z0 + v;
     C x[R], y[R];
 #pragma unroll
@@ -262,7 +265,7 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
       if (j * S + S - 1 < Nh || k1 < Nh) {
         const C u = w0[(size_t)k1 * M + col], qv = w1[(size_t)k1 * M + col];
         const C m = C{u.x + qv.y, qv.x - u.y};
-        if (q == 0) {
+        if (self) {
           if (j == 0) {
             x[0] = C{u.x, qv.x};
           } else {
@@ -271,15 +274,16 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
           }
         } else {
           x[j] = C{u.x - qv.y, u.y + qv.x};
-          if (two) y[R - 1 - j] = m;
-          else x[R - 1 - j] = m;
+          y[R - 1 - j] = m;
         }
       }
       const int k2 = i2 + j * S;
-      if (two && (j * S + S - 1 < Nh || k2 < Nh)) {
+      if (j * S + S - 1 < Nh || k2 < Nh) {
         const C u = w0[(size_t)k2 * M + col], qv = w1[(size_t)k2 * M + col];
+        const C m = C{u.x + qv.y, qv.x - u.y};
         y[j] = C{u.x - qv.y, u.y + qv.x};
-        x[R - 1 - j] = C{u.x + qv.y, qv.x - u.y};
+        if (self) y[R - 1 - j] = m;
+        else x[R - 1 - j] = m;
       }
     }
     Dft<R, +1, C>::run(x);
@@ -289,9 +293,9 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
 #pragma unroll
       for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
     }
-    if (two) {
-      Dft<R, +1, C>::run(y);
-      pass_tw<PL, 0, +1>(y, tw, i2);
+    Dft<R, +1, C>::run(y);
+    pass_tw<PL, 0, +1>(y, tw, i2);
+    {
       C* p = sm + PL::phys(i2) * V + v;
 #pragma unroll
       for (int k = 0; k < R; ++k) p[k * SP * V] = y[k];
@@ -302,8 +306,9 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
 
 // Last forward DIT pass of the row kernel fused with the Hermitian unpack.
 // Butterfly i produces P[i + j S]; the conjugate partner P[M - i - j S] sits in
-// butterfly S - i at index R-1-j (or, for i = 0, in butterfly 0 at (R-j) mod R),
-// so one thread transforms the pair (i, S - i) and writes
+// butterfly S - i at index R-1-j (for i = 0 in butterfly 0 at (R-j) mod R, for
+// i = S/2 in butterfly S/2 at R-1-j), so one thread transforms the pair
+// (q, S - q), or (0, S/2) for q = 0, and writes
 // A = (P[k] + conj P[M-k]) / 2 and B = (P[k] - conj P[M-k]) / (2i) for k < N/2
 // straight to the work planes.  Outputs with N/2 <= k <= M - N/2 are never formed.
 template <typename T, class PL, int V, int NT>
@@ -314,16 +319,16 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
   constexpr int S = M / R;
   constexpr int SP = PL::pstride(0);
   constexpr int Nh = M / 3;
-  constexpr int NQ = S / 2 + 1;
-  static_assert(S % 2 == 0, "paired unpack needs an even stride");
+  constexpr int NQ = S / 2;
+  static_assert(S % 2 == 0 && R % 2 == 0, "paired unpack needs an even stride and radix");
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   C* __restrict__ w0 = static_cast<C*>(a.w0);
   C* __restrict__ w1 = static_cast<C*>(a.w1);
   for (int w = tid; w < V * NQ; w += NT) {
     const int v = w % V;
     const int q = w / V;
-    const bool two = q > 0 && 2 * q < S;
-    const int i2 = S - q;
+    const bool self = q == 0;
+    const int i2 = self ? S / 2 : S - q;
     C y1[R], y2[R];
     {
       const C* p = sm + PL::phys(q) * V + v;
@@ -332,15 +337,12 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
       pass_tw<PL, 0, -1>(y1, tw, q);
       Dft<R, -1, C>::run(y1);
     }
-    if (two) {
+    {
       const C* p = sm + PL::phys(i2) * V + v;
 #pragma unroll
       for (int k = 0; k < R; ++k) y2[k] = p[k * SP * V];
       pass_tw<PL, 0, -1>(y2, tw, i2);
       Dft<R, -1, C>::run(y2);
-    } else {
-#pragma unroll
-      for (int k = 0; k < R; ++k) y2[k] = C{T(0), T(0)};
     }
     const size_t col = (size_t)z0 + v;
 #pragma unroll
@@ -349,14 +351,14 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
       const int k1 = q + j * S;
       if (j * S + S - 1 < Nh || k1 < Nh) {
         const C p = y1[j];
-        const C c = (q == 0) ? y1[(R - j) % R] : (two ? y2[R - 1 - j] : y1[R - 1 - j]);
+        const C c = self ? y1[(R - j) % R] : y2[R - 1 - j];
         w0[(size_t)k1 * M + col] = C{T(0.5) * (p.x + c.x), T(0.5) * (p.y - c.y)};
         w1[(size_t)k1 * M + col] = C{T(0.5) * (p.y + c.y), T(-0.5) * (p.x - c.x)};
       }
       const int k2 = i2 + j * S;
-      if (two && (j * S + S - 1 < Nh || k2 < Nh)) {
+      if (j * S + S - 1 < Nh || k2 < Nh) {
         const C p = y2[j];
-        const C c = y1[R - 1 - j];
+        const C c = self ? y2[R - 1 - j] : y1[R - 1 - j];
         w0[(size_t)k2 * M + col] = C{T(0.5) * (p.x + c.x), T(0.5) * (p.y - c.y)};
         w1[(size_t)k2 * M + col] = C{T(0.5) * (p.y + c.y), T(-0.5) * (p.x - c.x)};
       }

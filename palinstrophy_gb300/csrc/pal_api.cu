@@ -45,6 +45,7 @@ struct pal_handle {
   int row_idx = 0, col_idx = 0;
   cudaStream_t stream = nullptr;
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
+  void *om_p = nullptr, *fm_p = nullptr;  // om / fnm1 in butterfly-major order, used inside pal_step
   void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
   void *vis_w = nullptr;      // two scratch work planes for display transforms
@@ -95,6 +96,8 @@ StepArgs base_args(pal_handle* h) {
   a.sc = h->sc;
   a.part = h->part;
   a.phys = h->phys;
+  a.om_p = h->om_p;
+  a.fm_p = h->fm_p;
   a.N = h->N;
   return a;
 }
@@ -121,7 +124,10 @@ int launch_row(pal_handle* h, int flags) {
   return PAL_OK;
 }
 
-int launch_col(pal_handle* h, int scheme, int stage, int flags) {
+// `perm`: the column pass on om_p / fm_p (butterfly-major om, fnm1), whose
+// update reads and writes om / fnm1 with coalesced accesses; pal_step converts
+// to that order on entry and back on exit (om_layout).
+int launch_col(pal_handle* h, int scheme, int stage, int flags, bool perm = false) {
   StepArgs a = base_args(h);
   a.tw = h->tw_col;
   a.flags = flags;
@@ -130,7 +136,10 @@ int launch_col(pal_handle* h, int scheme, int stage, int flags) {
     a.alpha = kRkAlpha[stage];
     a.beta = kRkBeta[stage];
   }
-  h->ck->col(a, h->stream);
+  if (perm)
+    h->ck->col_perm(a, h->stream);
+  else
+    h->ck->col(a, h->stream);
   PAL_LAUNCHED(h, "k_col");
   h->state = ST_U;
   return PAL_OK;
@@ -153,17 +162,28 @@ int read_scalars(pal_handle* h) {
   return PAL_OK;
 }
 
+// om / fnm1 from the natural columns into om_p / fm_p (to_perm) or back.
+int om_layout(pal_handle* h, bool to_perm) {
+  StepArgs a = base_args(h);
+  if (to_perm)
+    h->ck->to_perm(a, h->stream);
+  else
+    h->ck->from_perm(a, h->stream);
+  PAL_LAUNCHED(h, "k_om_perm");
+  return PAL_OK;
+}
+
 // One full step; the first row pass carries a deferred NEXTDT when `dt_update`.
-int one_step(pal_handle* h, int method, bool dt_update, bool advance) {
+int one_step(pal_handle* h, int method, bool dt_update, bool advance, bool perm = false) {
   const int rflags = dt_update ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
   int rc;
   if (method == PAL_CNAB2) {
     if ((rc = launch_row(h, rflags))) return rc;
-    return launch_col(h, 0, 0, pal::F_CNM1 | (advance ? pal::F_ADVANCE : 0));
+    return launch_col(h, 0, 0, pal::F_CNM1 | (advance ? pal::F_ADVANCE : 0), perm);
   }
   for (int s = 0; s < 3; ++s) {
     if ((rc = launch_row(h, s == 0 ? rflags : 0))) return rc;
-    if ((rc = launch_col(h, 1, s, (s == 2 && advance) ? pal::F_ADVANCE : 0))) return rc;
+    if ((rc = launch_col(h, 1, s, (s == 2 && advance) ? pal::F_ADVANCE : 0, perm))) return rc;
   }
   return PAL_OK;
 }
@@ -232,9 +252,9 @@ int autotune(pal_handle* h) {
       StepArgs a = base_args(h);
       a.tw = h->tw_col;
       a.scheme = 1;
-      h->ck->col(a, h->stream);
+      h->ck->col_perm(a, h->stream);
       cudaEventRecord(e0, h->stream);
-      for (int q = 0; q < reps; ++q) h->ck->col(a, h->stream);
+      for (int q = 0; q < reps; ++q) h->ck->col_perm(a, h->stream);
       cudaEventRecord(e1, h->stream);
       PAL_LAUNCHED(h, "autotune k_col");
       PAL_CK(h, cudaEventSynchronize(e1));
@@ -323,14 +343,16 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   h->spectral_blocks = std::max(1, std::min(4 * sms, (int)(((size_t)N * h->Nh + 255) / 256)));
   const size_t part_n = (size_t)std::max(h->M, std::max(1024, h->spectral_blocks)) * 5;
-  void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw_row, &h->tw_col};
-  const size_t sizes[] = {plane_w, plane_w, plane_om, plane_om, 2 * plane_om, tw_max * h->esz, tw_max * h->esz};
-  for (int i = 0; i < 7; ++i) {
+  void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw_row, &h->tw_col, &h->om_p};
+  const size_t sizes[] = {plane_w,           plane_w,           plane_om, plane_om, 2 * plane_om,
+                          tw_max * h->esz, tw_max * h->esz, 2 * plane_w};
+  for (int i = 0; i < 8; ++i) {
     e = cudaMalloc(bufs[i], sizes[i]);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc state"));
     e = cudaMemsetAsync(*bufs[i], 0, sizes[i], h->stream);
     if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMemset state"));
   }
+  h->fm_p = static_cast<char*>(h->om_p) + plane_w;
   e = cudaMalloc(&h->sc, sizeof(DevScalars));
   if (e != cudaSuccess) return bail(cuda_fail(nullptr, e, "cudaMalloc scalars"));
   e = cudaMalloc(&h->part, part_n * sizeof(double));
@@ -356,8 +378,8 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
 int pal_destroy(pal_handle* h) {
   if (!h) return PAL_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* bufs[] = {h->w0,     h->w1,   h->om,   h->fnm1, h->stage, h->tw_row,
-                  h->tw_col, h->phys, h->sc,   h->part, h->vis_w, h->vis_phys};
+  void* bufs[] = {h->w0,     h->w1,   h->om,   h->fnm1, h->stage, h->tw_row,   h->tw_col,
+                  h->phys,   h->sc,   h->part, h->vis_w, h->vis_phys, h->om_p};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->sc_host) cudaFreeHost(h->sc_host);
@@ -495,11 +517,19 @@ int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update
   if (int rc = resolve_velocity(h)) return rc;
   if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "pal_step needs the physical velocity");
   bool pending = false;
-  for (int j = 1; j <= nsteps; ++j) {
-    const long long it = h->it + 1;
-    if (int rc = one_step(h, method, pending, true)) return rc;
-    h->it = it;
-    pending = update > 0 && (it % update == 0 || it == 1 || (final_update && j == nsteps));
+  if (nsteps > 0) {
+    if (int rc = om_layout(h, true)) return rc;
+    int rc = PAL_OK;
+    for (int j = 1; j <= nsteps && rc == PAL_OK; ++j) {
+      const long long it = h->it + 1;
+      rc = one_step(h, method, pending, true, true);
+      if (rc != PAL_OK) break;
+      h->it = it;
+      pending = update > 0 && (it % update == 0 || it == 1 || (final_update && j == nsteps));
+    }
+    const int rc2 = om_layout(h, false);
+    if (rc != PAL_OK) return rc;
+    if (rc2 != PAL_OK) return rc2;
   }
   if (pending) return launch_phys(h, pal::F_UPDATE_DT);
   return PAL_OK;
@@ -840,6 +870,7 @@ int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, d
     }
   }
   int k = 0;
+  if (rc == PAL_OK) rc = om_layout(h, true);  // the pass as pal_step runs it
   if (rc == PAL_OK) {
     cudaEventRecord(ev[k++], h->stream);
     for (int j = 0; j < nsteps && rc == PAL_OK; ++j) {
@@ -848,11 +879,13 @@ int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, d
         cudaEventRecord(ev[k++], h->stream);
         if (rc == PAL_OK)
           rc = launch_col(h, method == PAL_CNAB2 ? 0 : 1, s,
-                          (method == PAL_CNAB2 ? pal::F_CNM1 : 0) | (s == stages - 1 ? pal::F_ADVANCE : 0));
+                          (method == PAL_CNAB2 ? pal::F_CNM1 : 0) | (s == stages - 1 ? pal::F_ADVANCE : 0), true);
         cudaEventRecord(ev[k++], h->stream);
       }
       if (rc == PAL_OK) h->it += 1;
     }
+    const int rc2 = om_layout(h, false);
+    if (rc == PAL_OK) rc = rc2;
   }
   double tr = 0.0, tc = 0.0;
   if (rc == PAL_OK) {

@@ -210,6 +210,27 @@ struct Plan {
     freq_digits<0>(pos, f);
     return f;
   }
+  // Butterfly-major order of the DIF output.  The butterfly b of the last DIF
+  // pass holds the frequencies freq(b RP) + j FSTEP, j < RP; mid_perm(f) is the
+  // index j FSTEP + b of frequency f, so that consecutive butterflies (lanes)
+  // visiting the same j touch consecutive indices.
+  static constexpr int FSTEP = M / RP;
+  template <int Q>
+  static __device__ __forceinline__ void perm_digits(int& f, int& pos) {
+    if constexpr (Q >= 0) {
+      constexpr int w = weight(Q);
+      constexpr int s = stride(Q);
+      const int k = f / w;
+      f -= k * w;
+      pos += k * s;
+      perm_digits<Q - 1>(f, pos);
+    }
+  }
+  static __device__ __forceinline__ int mid_perm(int f) {
+    int pos = 0;
+    perm_digits<NP - 1>(f, pos);
+    return (pos % RP) * FSTEP + pos / RP;
+  }
 };
 
 // The same plan with compact twiddle tables: per pass and butterfly only

@@ -65,6 +65,8 @@ struct StepArgs {
   const void* y0;   // adjoint: the forward velocity planes of the stage
   const void* y1;
   int ahead;        // resident blocks of one wave (L2-prefetch candidates; 0 = none)
+  void* om_p;       // om / fnm1 in the column plan's butterfly-major order (N/2 x M)
+  void* fm_p;
 };
 
 // Member view of the arguments for block row blockIdx.y.
@@ -549,7 +551,9 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
 // and results by shuffle.  When 3 divides the radix, the de-aliased band
 // (frequencies N/2 .. N-1, the middle third of the positions) is known at
 // compile time and skipped.  om / fm are read from s_om / s_fm when SMEM_OM.
-template <typename T, class PL, int NT, bool SMEM_OM>
+// With PERM, om / fm are columns in butterfly-major order (Plan::mid_perm):
+// the lanes of a warp then read and write consecutive elements.
+template <typename T, class PL, int NT, bool SMEM_OM, bool PERM>
 __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
                                            cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
                                            const ModeCoef<T>& cf, int kx, int tid) {
@@ -591,9 +595,10 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       const bool inband = act && (BAND_CT || f < Nh || f >= N);
       const int z = f < Nh ? f : f - Nh;
       C uh = {T(0), T(0)}, vh = {T(0), T(0)};
+      const int zi = PERM ? (j + v) * FSTEP + b : z;
       if (inband) {
-        const C o = SMEM_OM ? s_om[z] : om[z];
-        const C fo = SMEM_OM ? s_fm[z] : fm[z];
+        const C o = SMEM_OM ? s_om[z] : om[zi];
+        const C fo = SMEM_OM ? s_fm[z] : fm[zi];
         const T gz = T(z < Nh ? z : z - N);
         const T K2 = ax * ax + gz * gz;
         const T GA = gz * ax;
@@ -608,8 +613,8 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
         C on;
         on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
         on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
-        om[z] = on;
-        fm[z] = fn;
+        om[zi] = on;
+        fm[zi] = fn;
         if (kx >= 1) {
           const T ik = T(1) / K2;
           const C t = {on.x * ik, on.y * ik};
@@ -679,8 +684,9 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
 
 // k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF == 1
 // the column's om and fnm1 are copied into shared memory asynchronously at
-// entry, so the update reads them without exposed global latency.
-template <typename T, class PL, int NT, int PREF>
+// entry, so the update reads them without exposed global latency.  With PERM
+// the kernel works on om_p / fm_p (butterfly-major columns of M elements).
+template <typename T, class PL, int NT, int PREF, bool PERM>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
@@ -694,11 +700,11 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   C* __restrict__ w0 = static_cast<C*>(a.w0);
   C* __restrict__ w1 = static_cast<C*>(a.w1);
-  C* __restrict__ om = static_cast<C*>(a.om) + (size_t)kx * N;
-  C* __restrict__ fm = static_cast<C*>(a.fnm1) + (size_t)kx * N;
+  C* __restrict__ om = PERM ? static_cast<C*>(a.om_p) + (size_t)kx * M : static_cast<C*>(a.om) + (size_t)kx * N;
+  C* __restrict__ fm = PERM ? static_cast<C*>(a.fm_p) + (size_t)kx * M : static_cast<C*>(a.fnm1) + (size_t)kx * N;
   C* s_om = sm + PL::PADM * V;
   C* s_fm = s_om + N;
-  if constexpr (PREF == 1) {
+  if constexpr (PREF == 1 && !PERM) {
     constexpr int CH = N * (int)sizeof(C) / 16;
     for (int c = tid; c < 2 * CH; c += NT) {
       const bool second = c >= CH;
@@ -730,14 +736,39 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     __syncthreads();
   }
   dif_range<T, PL, V, NT, -1, 1, PL::NP - 1>(sm, tw, tid);
-  if constexpr (PREF == 1) {
+  if constexpr (PREF == 1 && !PERM) {
     cp_async_wait_all();
     __syncthreads();
   }
-  col_middle<T, PL, NT, PREF == 1>(sm, s_om, s_fm, om, fm, cf, kx, tid);
+  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM>(sm, s_om, s_fm, om, fm, cf, kx, tid);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
   col_finish<NT>(a, tid);
+}
+
+// om / fnm1 between the natural [kx][z] columns and the butterfly-major
+// columns of the column plan PL (om_p, fm_p; only the N in-band entries of each
+// M-element column are written or read).  One block per kx column.
+template <typename T, class PL, bool TO_PERM>
+__global__ void __launch_bounds__(256) k_om_perm(StepArgs a0) {
+  using C = cplx<T>;
+  const StepArgs a = member_args(a0, sizeof(C));
+  constexpr int M = PL::M, N = 2 * M / 3, Nh = M / 3;
+  const int kx = blockIdx.x;
+  C* __restrict__ no = static_cast<C*>(a.om) + (size_t)kx * N;
+  C* __restrict__ nf = static_cast<C*>(a.fnm1) + (size_t)kx * N;
+  C* __restrict__ po = static_cast<C*>(a.om_p) + (size_t)kx * M;
+  C* __restrict__ pf = static_cast<C*>(a.fm_p) + (size_t)kx * M;
+  for (int z = threadIdx.x; z < N; z += 256) {
+    const int p = PL::mid_perm(z < Nh ? z : z + Nh);
+    if constexpr (TO_PERM) {
+      po[p] = no[z];
+      pf[p] = nf[z];
+    } else {
+      no[z] = po[p];
+      nf[z] = pf[p];
+    }
+  }
 }
 
 // k_col_inv: velocity low band -> pad -> inverse z-FFT -> U planes.  The low

@@ -32,6 +32,11 @@ struct ColKernels {
   void (*col)(const StepArgs&, cudaStream_t);
   void (*col_inv)(const StepArgs&, cudaStream_t);
   void (*twiddles)(void* tw, cudaStream_t);
+  // the same pass on butterfly-major om / fnm1 (a.om_p, a.fm_p), and the
+  // conversions between that order and the natural columns
+  void (*col_perm)(const StepArgs&, cudaStream_t);
+  void (*to_perm)(const StepArgs&, cudaStream_t);
+  void (*from_perm)(const StepArgs&, cudaStream_t);
 };
 
 // Adjoint of one LS-IMEX-RK3 stage (pal_adjoint.cuh), on fixed plans.
@@ -113,24 +118,27 @@ struct ColOf {
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
   static constexpr size_t smem = smem_inv + (PREF == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
-  static inline int ahead = 0;
   static cudaError_t configure() {
     cudaError_t e =
-        cudaFuncSetAttribute(k_col<T, PL, NT, PREF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_col<T, PL, NT, PREF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (PREF == 2) ahead = wave_blocks(k_col<T, PL, NT, PREF>, NT, smem);
+    e = cudaFuncSetAttribute(k_col<T, PL, NT, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
-  static void col(const StepArgs& a, cudaStream_t s) {
-    StepArgs b = a;
-    b.ahead = ahead;
-    k_col<T, PL, NT, PREF><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem, s>>>(b);
+  static dim3 grid(const StepArgs& a) { return dim3(a.N / 2, a.members > 1 ? a.members : 1); }
+  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF, false><<<grid(a), NT, smem, s>>>(a); }
+  static void col_perm(const StepArgs& a, cudaStream_t s) {
+    k_col<T, PL, NT, 0, true><<<grid(a), NT, smem_inv, s>>>(a);
   }
+  static void to_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, true><<<grid(a), 256, 0, s>>>(a); }
+  static void from_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, false><<<grid(a), 256, 0, s>>>(a); }
   static void col_inv(const StepArgs& a, cudaStream_t s) {
     k_col_inv<T, PL, NT><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem_inv, s>>>(a);
   }
   static constexpr ColKernels make(const char* name) {
-    return ColKernels{name, NT, smem, PL::TW_TOTAL, configure, col, col_inv, launch_twiddles<T, PL>};
+    return ColKernels{name,    NT,     smem,     PL::TW_TOTAL,          configure, col,
+                      col_inv, launch_twiddles<T, PL>, col_perm, to_perm, from_perm};
   }
 };
 

@@ -445,7 +445,9 @@ def run_gb300(args):
         "fp32_over_fp64": rate32 / rate64,
         "rel_l2_fp32_vs_fp64_100_steps": rel,
         "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 6 * args.steps + (args.steps // UPDATE + 1),
+        # timed region = one pal_step call: 6 launches per RK3 step, the two om/fnm1
+        # order conversions, and a k_phys launch if the last step ends on the NEXTDT cadence
+        "gpu_launches": 6 * args.steps + 2 + int((args.warmup + args.steps) % UPDATE == 0),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(dominant, "fp32"), "algorithmic_bytes": dom_bytes,

@@ -38,6 +38,7 @@ struct Group {
   std::vector<int> members;  // global member indices, local order
   std::vector<char> has_vel;  // velocity band uploaded for this member
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr, *vel = nullptr;
+  void *om_p = nullptr, *fm_p = nullptr;  // butterfly-major om / fnm1 used during pal_ensemble_step
   void *tw_row = nullptr, *tw_col = nullptr, *phys = nullptr;
   DevScalars* sc = nullptr;
   double* part = nullptr;
@@ -101,6 +102,8 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
   a.sc = g.sc;
   a.part = g.part;
   a.phys = g.phys;
+  a.om_p = g.om_p;
+  a.fm_p = g.fm_p;
   a.N = g.N;
   a.members = (int)g.members.size();
   a.ms_w = (long long)g.Nh * g.M;
@@ -112,6 +115,21 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
   return a;
 }
 
+// om / fnm1 of every group into butterfly-major order (to_perm) or back.
+int om_layout(pal_ensemble* e, bool to_perm) {
+  for (Group& g : e->groups) {
+    StepArgs a = group_args(e, g);
+    if (to_perm)
+      g.ck->to_perm(a, e->stream);
+    else
+      g.ck->from_perm(a, e->stream);
+  }
+  cudaError_t c = cudaGetLastError();
+  if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble om order: ") + cudaGetErrorString(c));
+  return PAL_OK;
+}
+
+// One step of every group; the column pass works on the butterfly-major om / fnm1.
 int launch_step(pal_ensemble* e, int method, bool dt_update) {
   const int stages = method == PAL_CNAB2 ? 1 : 3;
   for (int s = 0; s < stages; ++s) {
@@ -129,7 +147,7 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
         a.beta = kRkBeta[s];
       }
       a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
-      g.ck->col(a, e->stream);
+      g.ck->col_perm(a, e->stream);
     }
   }
   cudaError_t c = cudaGetLastError();
@@ -204,15 +222,16 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
     const size_t nm = g.members.size();
     const size_t plane_w = (size_t)g.Nh * g.M * e->esz, plane_om = (size_t)g.Nh * g.N * e->esz;
     g.part_stride = std::max<long long>(2LL * g.M, 5 * 1024);
-    void** bufs[] = {&g.w0, &g.w1, &g.om, &g.fnm1, &g.vel, &g.tw_row, &g.tw_col};
+    void** bufs[] = {&g.w0, &g.w1, &g.om, &g.fnm1, &g.vel, &g.tw_row, &g.tw_col, &g.om_p};
     const size_t sizes[] = {nm * plane_w, nm * plane_w, nm * plane_om, nm * plane_om, 2 * nm * plane_om,
-                            (size_t)g.rk->tw_elems * e->esz, (size_t)g.ck->tw_elems * e->esz};
-    for (int i = 0; i < 7; ++i) {
+                            (size_t)g.rk->tw_elems * e->esz, (size_t)g.ck->tw_elems * e->esz, 2 * nm * plane_w};
+    for (int i = 0; i < 8; ++i) {
       c = cudaMalloc(bufs[i], sizes[i]);
       if (c == cudaSuccess) c = cudaMemsetAsync(*bufs[i], 0, sizes[i], e->stream);
       if (c != cudaSuccess) return bail(efail(nullptr, c == cudaErrorMemoryAllocation ? PAL_ERR_OOM : PAL_ERR_CUDA,
                                               std::string("ensemble alloc: ") + cudaGetErrorString(c)));
     }
+    g.fm_p = static_cast<char*>(g.om_p) + nm * plane_w;
     c = cudaMalloc(&g.sc, nm * sizeof(DevScalars));
     if (c == cudaSuccess) c = cudaMalloc(&g.part, nm * g.part_stride * sizeof(double));
     if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_OOM, "ensemble scalars"));
@@ -246,7 +265,7 @@ int pal_ensemble_destroy(pal_ensemble* e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
   for (Group& g : e->groups) {
-    void* bufs[] = {g.w0, g.w1, g.om, g.fnm1, g.vel, g.tw_row, g.tw_col, g.phys, g.sc, g.part};
+    void* bufs[] = {g.w0, g.w1, g.om, g.fnm1, g.vel, g.tw_row, g.tw_col, g.phys, g.sc, g.part, g.om_p};
     for (void* b : bufs)
       if (b) cudaFree(b);
   }
@@ -346,8 +365,10 @@ int pal_ensemble_step(pal_ensemble* e, int method, int nsteps, int update, int u
   upd[nsteps] = pending;
   for (bool b : upd) key += b ? '1' : '0';
   auto record = [&]() -> int {
+    if (int rc = om_layout(e, true)) return rc;
     for (int j = 0; j < nsteps; ++j)
       if (int rc = launch_step(e, method, upd[j])) return rc;
+    if (int rc = om_layout(e, false)) return rc;
     if (upd[nsteps])
       if (int rc = launch_stats(e, pal::F_UPDATE_DT)) return rc;
     return PAL_OK;

@@ -78,6 +78,8 @@ __device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz) {
   b.w1 = static_cast<char*>(a.w1) + m * a.ms_w * esz;
   b.om = static_cast<char*>(a.om) + m * a.ms_om * esz;
   b.fnm1 = static_cast<char*>(a.fnm1) + m * a.ms_om * esz;
+  if (a.om_p) b.om_p = static_cast<char*>(a.om_p) + m * a.ms_w * esz;  // N/2 x M per member, as w0
+  if (a.fm_p) b.fm_p = static_cast<char*>(a.fm_p) + m * a.ms_w * esz;
   if (a.phys) b.phys = static_cast<char*>(a.phys) + m * a.ms_phys * (esz / 2);
   if (a.src) b.src = static_cast<const char*>(a.src) + m * a.ms_src * esz;
   b.sc = a.sc + m;

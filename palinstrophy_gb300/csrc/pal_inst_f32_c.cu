@@ -10,23 +10,13 @@ using P6144c = Plan<6144, 24, 16, 16>;
 
 const RowKernels r4096[] = {RowOf<float, P6144, 4, 512>::make("16.16.24 V4x512"),
                             RowOf<float, Rec<P6144>, 4, 512>::make("16.16.24r V4x512"),
-                            RowOf<float, Rec<P6144>, 4, 512, 1>::make("16.16.24r V4x512 l2pf"),
-                            RowOf<float, Rec<P6144>, 4, 512, 2>::make("16.16.24r V4x512 paired"),
                             RowOf<float, Rec<P6144>, 4, 512, 3>::make("16.16.24r V4x512 paired l2pf"),
                             RowOf<float, Rec<P6144>, 4, 768, 3>::make("16.16.24r V4x768 paired l2pf"),
-                            RowOf<float, Rec<P6144>, 4, 768, 1>::make("16.16.24r V4x768 l2pf"),
                             RowOf<float, Rec<P6144>, 4, 1024, 3>::make("16.16.24r V4x1024 paired l2pf"),
-                            RowOf<float, Rec<P6144>, 4, 1024, 1>::make("16.16.24r V4x1024 l2pf"),
-                            RowOf<float, Rec<P6144b>, 4, 512, 2>::make("32.8.24r V4x512 paired"),
-                            RowOf<float, Rec<P6144c>, 4, 512>::make("24.16.16r V4x512"),
-                            RowOf<float, P6144, 2, 256>::make("16.16.24 V2x256")};
+                            RowOf<float, Rec<P6144b>, 4, 512, 2>::make("32.8.24r V4x512 paired")};
 const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
-                            ColOf<float, P6144b, 256>::make("32.8.24 x256"),
-                            ColOf<float, P6144c, 256>::make("24.16.16 x256"),
                             ColOf<float, Rec<P6144c>, 256>::make("24.16.16r x256"),
                             ColOf<float, Rec<P6144>, 256>::make("16.16.24r x256"),
-                            ColOf<float, Rec<P6144c>, 512, 1>::make("24.16.16r x512 pref"),
-                            ColOf<float, Rec<P6144>, 512, 1>::make("16.16.24r x512 pref"),
                             ColOf<float, Rec<P6144c>, 384>::make("24.16.16r x384"),
                             ColOf<float, Rec<P6144>, 384>::make("16.16.24r x384")};
 

@@ -35,13 +35,15 @@ const ColKernels c2048[] = {ColOf<float, P3072, 256>::make("16.8.24 x256"), ColO
                             ColOf<float, P3072b, 256>::make("8.16.24 x256"),
                             ColOf<float, Rec<P3072b>, 256>::make("8.16.24r x256"),
                             ColOf<float, Rec<P3072b>, 256, 1>::make("8.16.24r x256 pref"),
-                            ColOf<float, Rec<P3072b>, 512, 1>::make("8.16.24r x512 pref")};
+                            ColOf<float, Rec<P3072b>, 512, 1>::make("8.16.24r x512 pref"),
+                            ColOf<float, Rec<P3072b>, 256, 2>::make("8.16.24r x256 hoist")};
 const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512"),
                             RowOf<float, Rec<P4608>, 4, 576, 3>::make("16.12.24r V4x576 paired l2pf"),
                             RowOf<float, Rec<P4608>, 4, 512, 3>::make("16.12.24r V4x512 paired l2pf"),
                             RowOf<float, P4608, 2, 256>::make("16.12.24 V2x256")};
 const ColKernels c3072[] = {ColOf<float, P4608, 256>::make("16.12.24 x256"), ColOf<float, P4608, 512>::make("16.12.24 x512"),
-                            ColOf<float, Rec<P4608>, 256>::make("16.12.24r x256")};
+                            ColOf<float, Rec<P4608>, 256>::make("16.12.24r x256"),
+                            ColOf<float, Rec<P4608>, 256, 2>::make("16.12.24r x256 hoist")};
 
 PAL_KERNEL_SET(float, 0, 1024, r1024, c1024)
 PAL_KERNEL_SET(float, 0, 1536, r1536, c1536)

@@ -554,8 +554,11 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
 // (frequencies N/2 .. N-1, the middle third of the positions) is known at
 // compile time and skipped.  om / fm are read from s_om / s_fm when SMEM_OM.
 // With PERM, om / fm are columns in butterfly-major order (Plan::mid_perm):
-// the lanes of a warp then read and write consecutive elements.
-template <typename T, class PL, int NT, bool SMEM_OM, bool PERM>
+// the lanes of a warp then read and write consecutive elements.  With HOIST a
+// lane requests all its om / fm values before the butterfly's shared-memory
+// loads and DFT, so their latency overlaps that work (the update loop stores
+// to om / fm, so the compiler cannot move later loads above earlier stores).
+template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false>
 __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
                                            cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
                                            const ModeCoef<T>& cf, int kx, int tid) {
@@ -575,6 +578,23 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
     const int b = act ? (w >> 1) : 0;
     C* p = sm + b * (R + 1) * V + v;
     const int fb = PL::freq(b * R);
+    constexpr int NH = HOIST ? R / 2 : 1;
+    C h_o[NH], h_f[NH];
+    if constexpr (HOIST) {
+#pragma unroll
+      for (int jj = 0; jj < R / 2; ++jj) {
+        const int j = 2 * jj;
+        h_o[jj] = h_f[jj] = C{T(0), T(0)};
+        if (BAND_CT && j >= R / 3 && j < 2 * R / 3) continue;
+        const int f = fb + (j + v) * FSTEP;
+        const int z = f < Nh ? f : f - Nh;
+        const int zi = PERM ? (j + v) * FSTEP + b : z;
+        if (act && (BAND_CT || f < Nh || f >= N)) {
+          h_o[jj] = om[zi];
+          h_f[jj] = fm[zi];
+        }
+      }
+    }
     C x[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) x[j] = act ? p[j * V] : C{T(0), T(0)};
@@ -599,8 +619,8 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       C uh = {T(0), T(0)}, vh = {T(0), T(0)};
       const int zi = PERM ? (j + v) * FSTEP + b : z;
       if (inband) {
-        const C o = SMEM_OM ? s_om[z] : om[zi];
-        const C fo = SMEM_OM ? s_fm[z] : fm[zi];
+        const C o = SMEM_OM ? s_om[z] : (HOIST ? h_o[j / 2] : om[zi]);
+        const C fo = SMEM_OM ? s_fm[z] : (HOIST ? h_f[j / 2] : fm[zi]);
         const T gz = T(z < Nh ? z : z - N);
         const T K2 = ax * ax + gz * gz;
         const T GA = gz * ax;
@@ -686,8 +706,9 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
 
 // k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF == 1
 // the column's om and fnm1 are copied into shared memory asynchronously at
-// entry, so the update reads them without exposed global latency.  With PERM
-// the kernel works on om_p / fm_p (butterfly-major columns of M elements).
+// entry, so the update reads them without exposed global latency; PREF == 2
+// hoists each lane's om / fnm1 loads above its DFT (col_middle HOIST).  With
+// PERM the kernel works on om_p / fm_p (butterfly-major columns of M elements).
 template <typename T, class PL, int NT, int PREF, bool PERM>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
@@ -742,7 +763,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     cp_async_wait_all();
     __syncthreads();
   }
-  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM>(sm, s_om, s_fm, om, fm, cf, kx, tid);
+  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2>(sm, s_om, s_fm, om, fm, cf, kx, tid);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
   col_finish<NT>(a, tid);

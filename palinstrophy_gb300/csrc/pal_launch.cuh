@@ -117,19 +117,22 @@ template <typename T, class PL, int NT, int PREF = 0>
 struct ColOf {
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
   static constexpr size_t smem = smem_inv + (PREF == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
+  // the butterfly-major variant has no shared-memory om staging (PREF 1)
+  static constexpr int PERM_PREF = PREF == 1 ? 0 : PREF;
   static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
   static cudaError_t configure() {
     cudaError_t e =
         cudaFuncSetAttribute(k_col<T, PL, NT, PREF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_col<T, PL, NT, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
+    e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_inv);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
   static dim3 grid(const StepArgs& a) { return dim3(a.N / 2, a.members > 1 ? a.members : 1); }
   static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF, false><<<grid(a), NT, smem, s>>>(a); }
   static void col_perm(const StepArgs& a, cudaStream_t s) {
-    k_col<T, PL, NT, 0, true><<<grid(a), NT, smem_inv, s>>>(a);
+    k_col<T, PL, NT, PERM_PREF, true><<<grid(a), NT, smem_inv, s>>>(a);
   }
   static void to_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, true><<<grid(a), 256, 0, s>>>(a); }
   static void from_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, false><<<grid(a), 256, 0, s>>>(a); }

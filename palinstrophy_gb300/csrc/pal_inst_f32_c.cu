@@ -21,7 +21,8 @@ const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
                             ColOf<float, Rec<P6144>, 384>::make("16.16.24r x384"),
                             ColOf<float, Rec<P6144>, 256, 2>::make("16.16.24r x256 hoist"),
                             ColOf<float, Rec<P6144c>, 256, 2>::make("24.16.16r x256 hoist"),
-                            ColOf<float, Rec<P6144>, 384, 2>::make("16.16.24r x384 hoist")};
+                            ColOf<float, Rec<P6144>, 256, 3>::make("16.16.24r x256 hoist pipe0"),
+                            ColOf<float, Rec<P6144c>, 256, 3>::make("24.16.16r x256 hoist pipe0")};
 
 PAL_KERNEL_SET(float, 0, 4096, r4096, c4096)
 }  // namespace

@@ -13,7 +13,8 @@ const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"
                             RowOf<float, Rec<P12288>, 2, 512, 3>::make("16.32.24r V2x512 paired l2pf")};
 const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
-                            ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist")};
+                            ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),
+                            ColOf<float, Rec<P12288>, 512, 3>::make("16.32.24r x512 hoist pipe0")};
 
 PAL_KERNEL_SET(float, 0, 8192, r8192, c8192)
 }  // namespace

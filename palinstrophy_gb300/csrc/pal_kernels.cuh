@@ -707,7 +707,8 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
 // k_col: P-state column -> (om, fnm1 update) -> U-state column.  With PREF == 1
 // the column's om and fnm1 are copied into shared memory asynchronously at
 // entry, so the update reads them without exposed global latency; PREF == 2
-// hoists each lane's om / fnm1 loads above its DFT (col_middle HOIST).  With
+// hoists each lane's om / fnm1 loads above its DFT (col_middle HOIST), PREF == 3
+// also overlaps the pass-0 loads of a thread's next butterfly.  With
 // PERM the kernel works on om_p / fm_p (butterfly-major columns of M elements).
 template <typename T, class PL, int NT, int PREF, bool PERM>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
@@ -739,8 +740,40 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   }
   const ModeCoef<T> cf = col_coef<T>(a, N);
 
-  // pass 0 (forward z-DIF) straight from the P planes
-  {
+  // pass 0 (forward z-DIF) straight from the P planes.  PREF == 3: the loads
+  // of a thread's next butterfly are issued before the current one's DFT.
+  if constexpr (PREF == 3 && (V * (M / PL::R[0])) % NT == 0) {
+    constexpr int R = PL::R[0];
+    constexpr int S = M / R;
+    constexpr int IT = V * S / NT;
+    C xn[R];
+    {
+      const C* __restrict__ src = ((tid & 1) == 0 ? w0 : w1) + (size_t)kx * M;
+#pragma unroll
+      for (int j = 0; j < R; ++j) xn[j] = src[(tid >> 1) + j * S];
+    }
+#pragma unroll 1
+    for (int it = 0; it < IT; ++it) {
+      const int w = tid + it * NT;
+      const int v = w & 1;
+      const int i = w >> 1;
+      C x[R];
+#pragma unroll
+      for (int j = 0; j < R; ++j) x[j] = xn[j];
+      if (it + 1 < IT) {
+        const int wn = w + NT;
+        const C* __restrict__ src = ((wn & 1) == 0 ? w0 : w1) + (size_t)kx * M;
+#pragma unroll
+        for (int j = 0; j < R; ++j) xn[j] = src[(wn >> 1) + j * S];
+      }
+      Dft<R, -1, C>::run(x);
+      pass_tw<PL, 0, -1>(x, tw, i);
+      C* p = sm + PL::phys(i) * V + v;
+#pragma unroll
+      for (int k = 0; k < R; ++k) p[k * PL::pstride(0) * V] = x[k];
+    }
+    __syncthreads();
+  } else {
     constexpr int R = PL::R[0];
     constexpr int S = M / R;
     for (int w = tid; w < V * S; w += NT) {
@@ -763,7 +796,7 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     cp_async_wait_all();
     __syncthreads();
   }
-  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2>(sm, s_om, s_fm, om, fm, cf, kx, tid);
+  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3>(sm, s_om, s_fm, om, fm, cf, kx, tid);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
   col_finish<NT>(a, tid);

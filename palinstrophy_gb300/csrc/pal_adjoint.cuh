@@ -43,7 +43,7 @@ __device__ __forceinline__ StageCoef<T> stage_coef(const StepArgs& a) {
 template <typename T, class PL, int NT>
 __global__ void __launch_bounds__(NT) k_adj_col_in(StepArgs a) {
   using C = cplx<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M, V = 2, N = 2 * M / 3, Nh = M / 3;
   const int tid = threadIdx.x, kx = blockIdx.x;
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(NT) k_adj_col_in(StepArgs a) {
 template <typename T, class PL, int V, int NT>
 __global__ void __launch_bounds__(NT) k_adj_row(StepArgs a) {
   using C = cplx<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* lam = reinterpret_cast<C*>(smraw);
   C* vel = lam + PL::PADM * V;
   constexpr int M = PL::M, Nh = M / 3;
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(NT) k_adj_row(StepArgs a) {
 template <typename T, class PL, int NT>
 __global__ void __launch_bounds__(NT) k_adj_col_out(StepArgs a) {
   using C = cplx<T>;
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M, V = 2, N = 2 * M / 3, Nh = M / 3;
   const int tid = threadIdx.x, kx = blockIdx.x;

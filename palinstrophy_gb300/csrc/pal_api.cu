@@ -1,5 +1,7 @@
 // C ABI of libpalgpu.so: handle-owned device state, stream-ordered launches of
 // the fused row/column kernels, and the reference-shaped entry points.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +48,7 @@ struct pal_handle {
   cudaStream_t stream = nullptr;
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
   void *om_p = nullptr, *fm_p = nullptr;  // om / fnm1 in butterfly-major order, used inside pal_step
+  pal::TmaMaps tmaps{};                   // w0 / w1 descriptors when the row candidate stores through TMA
   void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
   void *vis_w = nullptr;      // two scratch work planes for display transforms
@@ -59,6 +62,36 @@ struct pal_handle {
   int spectral_blocks = 0;
   std::string err;
 };
+
+namespace pal {
+
+bool encode_row_maps(TmaMaps* out, void* w0, void* w1, int N, int V, int members) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
+  const int M = 3 * N / 2, Nh = N / 2;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * M, (cuuint64_t)Nh, (cuuint64_t)members};
+  const cuuint64_t strides[2] = {(cuuint64_t)M * 8, (cuuint64_t)Nh * M * 8};  // bytes, dims 1 and 2
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * V), 256, 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  void* base[2] = {w0, w1};
+  CUtensorMap* maps[2] = {&out->w0, &out->w1};
+  for (int i = 0; i < 2; ++i) {
+    CUresult r = encode(maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base[i], dims, strides, box, elem,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+  }
+  return true;
+}
+
+}  // namespace pal
 
 namespace {
 
@@ -98,6 +131,7 @@ StepArgs base_args(pal_handle* h) {
   a.phys = h->phys;
   a.om_p = h->om_p;
   a.fm_p = h->fm_p;
+  a.tmaps = &h->tmaps;
   a.N = h->N;
   return a;
 }
@@ -201,6 +235,8 @@ int select_variant(pal_handle* h, int row, int col) {
   h->col_idx = col;
   h->rk = &h->ks->rows[row];
   h->ck = &h->ks->cols[col];
+  if (h->rk->tma && !pal::encode_row_maps(&h->tmaps, h->w0, h->w1, h->N, h->rk->V, 1))
+    return fail(h, PAL_ERR_CUDA, "TMA descriptor of the work planes could not be encoded");
   h->rk->twiddles(h->tw_row, h->stream);
   h->ck->twiddles(h->tw_col, h->stream);
   PAL_LAUNCHED(h, "twiddle tables");

@@ -39,6 +39,7 @@ struct Group {
   std::vector<char> has_vel;  // velocity band uploaded for this member
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr, *vel = nullptr;
   void *om_p = nullptr, *fm_p = nullptr;  // butterfly-major om / fnm1 used during pal_ensemble_step
+  pal::TmaMaps tmaps{};                   // w0 / w1 descriptors (member dimension = group size)
   void *tw_row = nullptr, *tw_col = nullptr, *phys = nullptr;
   DevScalars* sc = nullptr;
   double* part = nullptr;
@@ -104,6 +105,7 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
   a.phys = g.phys;
   a.om_p = g.om_p;
   a.fm_p = g.fm_p;
+  a.tmaps = &g.tmaps;
   a.N = g.N;
   a.members = (int)g.members.size();
   a.ms_w = (long long)g.Nh * g.M;
@@ -232,6 +234,8 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
                                               std::string("ensemble alloc: ") + cudaGetErrorString(c)));
     }
     g.fm_p = static_cast<char*>(g.om_p) + nm * plane_w;
+    if (g.rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, g.rk->V, (int)nm))
+      return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble TMA descriptors"));
     c = cudaMalloc(&g.sc, nm * sizeof(DevScalars));
     if (c == cudaSuccess) c = cudaMalloc(&g.part, nm * g.part_stride * sizeof(double));
     if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_OOM, "ensemble scalars"));

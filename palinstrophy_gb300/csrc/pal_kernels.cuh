@@ -16,6 +16,7 @@
 // maps onto this as: k_row = STEP2A row half + STEP2B products + STEP2B row
 // half; k_col = STEP2B column half + STEP3 + STEP2A column half.
 #pragma once
+#include <cuda.h>  // CUtensorMap (types only; descriptors are encoded through the runtime's driver entry point)
 #include <math.h>
 
 #include "pal_fft.cuh"
@@ -67,6 +68,14 @@ struct StepArgs {
   int ahead;        // resident blocks of one wave (L2-prefetch candidates; 0 = none)
   void* om_p;       // om / fnm1 in the column plan's butterfly-major order (N/2 x M)
   void* fm_p;
+  const struct TmaMaps* tmaps;  // host: descriptors of w0 / w1 for the row pass's bulk stores
+};
+
+// TMA descriptors of the two work planes, each a 3D view (2M floats, N/2 rows,
+// members) with a (2V floats, 256 rows, 1) box: one box is 256 rows of one row
+// tile.  Passed to the row kernel as a __grid_constant__ parameter.
+struct alignas(64) TmaMaps {
+  CUtensorMap w0, w1;
 };
 
 // Member view of the arguments for block row blockIdx.y.
@@ -370,6 +379,93 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
   }
 }
 
+// Bulk tensor stores (TMA) from shared memory.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int x, int y, int z) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map), "r"(s),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void tma_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// The paired last pass with the stores handed to the TMA unit: each thread
+// (one item, V S / 2 == NT) keeps its A, B rows in registers, the block
+// rewrites the tile as dense [plane][row][v] boxes and one thread issues the
+// bulk tensor stores, so no thread spends issue slots or LSU queue entries on
+// the plane writes and they drain while the next tile starts.
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_last_pass_tma(const StepArgs& a, cplx<T>* sm, int z0, int tid,
+                                                  const TmaMaps& maps) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  constexpr int SP = PL::pstride(0);
+  constexpr int Nh = M / 3;
+  constexpr int NQ = S / 2;
+  constexpr int JN = (Nh + S - 1) / S;  // j with j S < N/2
+  constexpr int BOX = 256;
+  static_assert(sizeof(C) == 8 && V * NQ == NT && Nh % BOX == 0, "one item per thread, FP32, whole boxes");
+  static_assert(size_t(2) * Nh * V <= size_t(PL::PADM) * V, "staging fits in the tile");
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  const int v = tid % V;
+  const int q = tid / V;
+  const bool self = q == 0;
+  const int i2 = self ? S / 2 : S - q;
+  C y1[R], y2[R];
+  {
+    const C* p = sm + PL::phys(q) * V + v;
+#pragma unroll
+    for (int k = 0; k < R; ++k) y1[k] = p[k * SP * V];
+    pass_tw<PL, 0, -1>(y1, tw, q);
+    Dft<R, -1, C>::run(y1);
+  }
+  {
+    const C* p = sm + PL::phys(i2) * V + v;
+#pragma unroll
+    for (int k = 0; k < R; ++k) y2[k] = p[k * SP * V];
+    pass_tw<PL, 0, -1>(y2, tw, i2);
+    Dft<R, -1, C>::run(y2);
+  }
+  C A1[JN], B1[JN], A2[JN], B2[JN];
+#pragma unroll
+  for (int j = 0; j < JN; ++j) {
+    const C p1 = y1[j], c1 = self ? y1[(R - j) % R] : y2[R - 1 - j];
+    A1[j] = C{T(0.5) * (p1.x + c1.x), T(0.5) * (p1.y - c1.y)};
+    B1[j] = C{T(0.5) * (p1.y + c1.y), T(-0.5) * (p1.x - c1.x)};
+    const C p2 = y2[j], c2 = self ? y2[R - 1 - j] : y1[R - 1 - j];
+    A2[j] = C{T(0.5) * (p2.x + c2.x), T(0.5) * (p2.y - c2.y)};
+    B2[j] = C{T(0.5) * (p2.y + c2.y), T(-0.5) * (p2.x - c2.x)};
+  }
+  __syncthreads();  // every read of the tile is done: reuse it as the staging area
+  C* stg = sm;      // [plane][k < N/2][v]
+#pragma unroll
+  for (int j = 0; j < JN; ++j) {
+    const int k1 = q + j * S, k2 = i2 + j * S;
+    if (k1 < Nh) {
+      stg[(size_t)k1 * V + v] = A1[j];
+      stg[(size_t)(Nh + k1) * V + v] = B1[j];
+    }
+    if (k2 < Nh) {
+      stg[(size_t)k2 * V + v] = A2[j];
+      stg[(size_t)(Nh + k2) * V + v] = B2[j];
+    }
+  }
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll 1
+    for (int bx = 0; bx < Nh / BOX; ++bx) {
+      tma_store_3d(&maps.w0, stg + (size_t)bx * BOX * V, 2 * z0, bx * BOX, (int)blockIdx.y);
+      tma_store_3d(&maps.w1, stg + (size_t)(Nh + bx * BOX) * V, 2 * z0, bx * BOX, (int)blockIdx.y);
+    }
+    tma_commit();
+    tma_wait_read();  // the shared memory stays the block's until the engine has read it
+  }
+}
+
 // L2 prefetch helpers.  `cp.async.bulk.prefetch.L2` pulls a contiguous,
 // 16-byte aligned range into L2 without occupying registers or the LSU queue;
 // `prefetch.global.L2` does one line.  Both are hints with no visible effect.
@@ -384,11 +480,12 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
 // PF bit 0: the tile one wave ahead (blockIdx.x + a.ahead) is pulled into L2
 // first, so that the block that will run it finds its rows there.
 // PF bit 1: the first pass reads every U-state row once (row_first_pass_paired).
+// PF bit 2 (value 4): the last pass stores through the TMA unit (row_last_pass_tma).
 template <typename T, class PL, int V, int NT, int PF>
-__global__ void __launch_bounds__(NT) k_row(StepArgs a0) {
+__global__ void __launch_bounds__(NT) k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   const int tid = threadIdx.x;
@@ -449,7 +546,10 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a0) {
   }
   if constexpr (sizeof(C) == 8) {
     dit_range<T, PL, V, NT, -1, PL::NP - 2, 1>(sm, tw, tid);
-    row_last_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
+    if constexpr ((PF & 4) != 0)
+      row_last_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps);
+    else
+      row_last_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
   } else {
     dit_range<T, PL, V, NT, -1, PL::NP - 2, 0>(sm, tw, tid);
     // unpack P = FFT(a + i b) into A = F(a), B = F(b) for kx < N/2 and store
@@ -473,7 +573,7 @@ template <typename T, class PL, int V, int NT>
 __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   const int tid = threadIdx.x;
@@ -714,7 +814,7 @@ template <typename T, class PL, int NT, int PREF, bool PERM>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   constexpr int V = 2;
@@ -835,7 +935,7 @@ template <typename T, class PL, int NT>
 __global__ void __launch_bounds__(NT) k_col_inv(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
-  extern __shared__ __align__(16) unsigned char smraw[];
+  extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   constexpr int V = 2;

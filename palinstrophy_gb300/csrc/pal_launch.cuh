@@ -15,6 +15,7 @@ namespace pal {
 struct RowKernels {
   const char* name;
   int V, NT;
+  bool tma;  // stores through TMA: the launch needs StepArgs::tmaps
   size_t smem;
   int tw_elems;
   cudaError_t (*configure)();
@@ -72,6 +73,11 @@ struct KernelSet {
 constexpr int kSpectralThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;
 
+// TMA descriptors of the planes w0 / w1 (members x N/2 rows x M complex FP32)
+// for a row candidate with tile height V; false if the driver call is missing
+// or refuses the layout.
+bool encode_row_maps(TmaMaps* out, void* w0, void* w1, int N, int V, int members);
+
 template <typename T, class PL>
 void launch_twiddles(void* tw, cudaStream_t s) {
   k_twiddles<T, PL><<<(PL::TW_TOTAL + 255) / 256, 256, 0, s>>>(static_cast<cplx<T>*>(tw));
@@ -103,13 +109,15 @@ struct RowOf {
   static void row(const StepArgs& a, cudaStream_t s) {
     StepArgs b = a;
     b.ahead = ahead;
-    k_row<T, PL, V, NT, PF><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(b);
+    static const TmaMaps none{};
+    k_row<T, PL, V, NT, PF><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
+        b, ((PF & 4) != 0 && a.tmaps) ? *a.tmaps : none);
   }
   static void phys(const StepArgs& a, cudaStream_t s) {
     k_phys<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
   }
   static constexpr RowKernels make(const char* name) {
-    return RowKernels{name, V, NT, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
+    return RowKernels{name, V, NT, (PF & 4) != 0, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
   }
 };
 

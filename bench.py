@@ -295,7 +295,7 @@ def _differentiation(directions=8):
     F.close()
     grad64 = grad64.astype(np.complex128)
     rng = np.random.default_rng(12345)
-    errs, errs64 = [], []
+    errs, errs64, fds, ads, ads64 = [], [], [], [], []
     for _ in range(directions):
         d = (rng.standard_normal(om0.shape) + 1j * rng.standard_normal(om0.shape)).astype(np.complex128)
         eps = 1e-3 * np.linalg.norm(om0) / np.linalg.norm(d)
@@ -310,14 +310,115 @@ def _differentiation(directions=8):
             G.close()
         fd = (vals[0] - vals[1]) / (2 * eps)
         ad = float(np.real(np.vdot(grad.astype(np.complex128), d)))
+        ad64 = float(np.real(np.vdot(grad64, d)))
         errs.append(abs(fd - ad) / abs(fd))
-        errs64.append(abs(fd - float(np.real(np.vdot(grad64, d)))) / abs(fd))
+        errs64.append(abs(fd - ad64) / abs(fd))
+        fds.append(fd)
+        ads.append(ad)
+        ads64.append(ad64)
     return {"N": N, "steps": nsteps, "checkpoint_every": ck, "precision": "fp32", "loss": loss,
             "forward_s": t_fwd, "gradient_call_s": t_grad,
             "backward_over_forward": (t_grad - t_fwd) / t_fwd,
             "fd_directions": directions, "fd_eps_rel": 1e-3, "fd_forward": "fp64",
             "fd_max_rel_err_fp32_adjoint": max(errs), "fd_max_rel_err_fp64_adjoint": max(errs64),
+            # the 8 directional derivatives as one vector: |ad - fd| / |fd|
+            "fd_rel_l2_fp32_adjoint": float(np.linalg.norm(np.subtract(ads, fds)) / np.linalg.norm(fds)),
+            "fd_rel_l2_fp64_adjoint": float(np.linalg.norm(np.subtract(ads64, fds)) / np.linalg.norm(fds)),
             "grad_rel_l2_fp32_vs_fp64_adjoint": float(np.linalg.norm(grad - grad64) / np.linalg.norm(grad64))}
+
+
+def _rel_l2(a, b):
+    import numpy as np
+    a = a.astype(np.complex128)
+    b = b.astype(np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _precision_form(steps=2000, update=100):
+    """N=1024, labelled k^4 exp(-2 (k/15)^2) unit-energy start (seed 4895), Re=1e4,
+    LS-IMEX-RK3 at CFL 0.1: the FP32 form and the FP64 plain path from the identical
+    start, each with its own adaptive dt; steps/s of each and their agreement."""
+    import numpy as np
+    import torch
+    from palinstrophy_gb300.initial import k4_unit_energy
+    from palinstrophy_gb300.turbo_simulator import Field
+    N, Re, cfl = 1024, 1e4, 0.1
+    om2, uc = k4_unit_energy(N, 15.0, SEED)
+    visc = float(np.float32(1.0 / float(np.float32(Re))))
+    out = {"N": N, "start": "k4_unit_energy(K0=15, seed 4895), labelled (not the reference generator)",
+           "method": METHOD, "cfl": cfl, "steps": steps, "update": update}
+    res = {}
+    for prec in ("fp32", "fp64"):
+        F = Field(N, prec, Re, cfl)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", visc)
+        F.step2a()
+        F.set_scalar("dt", cfl / (F.compute_cflm() * math.pi))
+        s = torch.cuda.ExternalStream(F.stream_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        F.synchronize()
+        e0.record(s)
+        F.step(METHOD, steps, update=update, final_update=True)
+        e1.record(s)
+        e1.synchronize()
+        d = F.diagnostics()
+        res[prec] = (F.om2(), d)
+        out[prec] = {"steps_per_s": steps / (e0.elapsed_time(e1) / 1000.0), "E": d["E"], "Z": d["Z"],
+                     "t": F.scalars()["t"]}
+        F.close()
+    out["rel_l2_om_fp32_vs_fp64"] = _rel_l2(res["fp32"][0], res["fp64"][0])
+    out["rel_E_fp32_vs_fp64"] = abs(res["fp32"][1]["E"] / res["fp64"][1]["E"] - 1.0)
+    out["rel_Z_fp32_vs_fp64"] = abs(res["fp32"][1]["Z"] / res["fp64"][1]["Z"] - 1.0)
+    return out
+
+
+def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100):
+    """N=8192 FP32 (KM3 K0=15 seed 4895, Re=1e5, LS-IMEX-RK3, CFL 0.1): steps/s and
+    per-kernel rates; and the energy / enstrophy history of the N=4096 FP32 form
+    against the FP64 plain run over 500 steps from the identical start."""
+    import torch
+    from palinstrophy_gb300 import _lib as L
+    from palinstrophy_gb300.turbo_simulator import Field
+    N = 8192
+    o8, u8, st8 = L.pao_generate(N, K0, RE, SEED, "KM3")
+    F = Field(N, "fp32", RE, CFL)
+    F.set_state(o8, None, u8)
+    F.set_scalar("visc", st8["visc"])
+    F.step2a()
+    F.set_scalar("dt", CFL / (F.compute_cflm() * math.pi))
+    ms_row, ms_col, _ = F.profile_kernels(METHOD, 3)
+    F.step(METHOD, 3, update=UPDATE)
+    s = torch.cuda.ExternalStream(F.stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    F.synchronize()
+    e0.record(s)
+    F.step(METHOD, steps_8192, update=UPDATE)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps_8192
+    variant = F.variant()["desc"]
+    F.close()
+    n2, s_bytes = float(N) * N, 4
+    big = {"N": N, "dtype": "f32", "steps": steps_8192, "steps_per_s": 1000.0 / ms, "ms_per_step": ms,
+           "kernels": variant,
+           "k_row": {"ms": ms_row, "algorithmic_GBps": 6.0 * n2 * s_bytes / (ms_row / 1000.0) / 1e9},
+           "k_col": {"ms": ms_col, "algorithmic_GBps": 10.0 * n2 * s_bytes / (ms_col / 1000.0) / 1e9}}
+    hist = {}
+    for prec in ("fp32", "fp64"):
+        G = _field(prec, om2, uc, visc)
+        h = []
+        for _ in range(drift_steps // every):
+            G.step(METHOD, every, update=UPDATE, final_update=True)
+            d = G.diagnostics()
+            h.append((d["E"], d["Z"]))
+        hist[prec] = h
+        G.close()
+    dE = max(abs(a[0] / b[0] - 1.0) for a, b in zip(hist["fp32"], hist["fp64"]))
+    dZ = max(abs(a[1] / b[1] - 1.0) for a, b in zip(hist["fp32"], hist["fp64"]))
+    drift = {"N": N_GRID, "steps": drift_steps, "every": every,
+             "E_fp64": [h[0] for h in hist["fp64"]], "Z_fp64": [h[1] for h in hist["fp64"]],
+             "max_rel_dE_fp32_vs_fp64": dE, "max_rel_dZ_fp32_vs_fp64": dZ}
+    return {"N8192_fp32": big, "N4096_fp32_vs_fp64_history": drift}
 
 
 def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
@@ -375,7 +476,6 @@ def run_gb300(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    from oracle import dns_oracle as do
     om2, uc, st = _init_arrays()
     visc = st["visc"]
 
@@ -405,13 +505,15 @@ def run_gb300(args):
     B = _field("fp64", om2, uc, visc)
     A.step(METHOD, 100, update=UPDATE, final_update=True)
     B.step(METHOD, 100, update=UPDATE, final_update=True)
-    rel = do.rel_l2(B.om2(), A.om2())
+    rel = _rel_l2(A.om2(), B.om2())
     A.close()
     B.close()
 
     e2e_rate, h2d, d2h = _e2e("fp32", om2, uc, visc, args.steps)
     ens = _ensemble_rate()
     diff = _differentiation()
+    prec_form = _precision_form()
+    large = _large_single_field(om2, uc, visc)
 
     rate32 = ws * args.steps / (ms32 / 1000.0)
     rate64 = ws * k64 / (ms64 / 1000.0)
@@ -455,6 +557,8 @@ def run_gb300(args):
                      "stage_bytes_per_s": (bytes_row + bytes_col) / ((ms_row + ms_col) / 1000.0) / 1e9},
         "ensemble": ens,
         "differentiation": diff,
+        "precision_form": prec_form,
+        "large_single_field": large,
         "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": min(8, os.cpu_count() or 1),
                          "kind": "port",
                          "sample": f"{cpu_n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up ({cpu_s:.1f} s), FP32 "

@@ -138,19 +138,71 @@ __device__ __forceinline__ void dft_ab(C* x) {
   }
 }
 
+// R = A*B with gcd(A, B) = 1 (Good-Thomas prime-factor mapping): input
+// n = (B n1 + A n2) mod R, output k with k = k1 (mod A), k = k2 (mod B).  Then
+// W_R^(n k) = W_A^(n1 k1) W_B^(n2 k2): a 2D DFT with no twiddles between the
+// factors; both index maps are compile-time register renamings.
+template <int A, int B>
+constexpr int crt_index(int k1, int k2) {
+  int k = 0;
+  while (k % A != k1 || k % B != k2) ++k;
+  return k;
+}
+// the output slot as a template constant, so no index is formed at run time
+template <int A, int B, int K1, int K2>
+struct Crt {
+  static constexpr int value = crt_index<A, B>(K1, K2);
+};
+template <int A, int B, int K1, typename C, int... K2>
+__device__ __forceinline__ void pfa_store(C* x, const C* t, std::integer_sequence<int, K2...>) {
+  ((x[Crt<A, B, K1, K2>::value] = t[K2]), ...);
+}
+template <int A, int B, int SIGN, typename C, int K1>
+__device__ __forceinline__ void pfa_column(C* x, const C* y) {
+  C t[B];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) t[n2] = y[n2 * A + K1];
+  Dft<B, SIGN, C>::run(t);
+  pfa_store<A, B, K1>(x, t, std::make_integer_sequence<int, B>{});
+}
+template <int A, int B, int SIGN, typename C, int... K1>
+__device__ __forceinline__ void pfa_columns(C* x, const C* y, std::integer_sequence<int, K1...>) {
+  (pfa_column<A, B, SIGN, C, K1>(x, y), ...);
+}
+template <int A, int B, int SIGN, typename C>
+__device__ __forceinline__ void dft_pfa(C* x) {
+  constexpr int R = A * B;
+  C y[R];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    C t[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) t[n1] = x[(B * n1 + A * n2) % R];
+    Dft<A, SIGN, C>::run(t);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = t[k1];
+  }
+  pfa_columns<A, B, SIGN, C>(x, y, std::make_integer_sequence<int, A>{});
+}
+
 #define PAL_COMPOSITE(R_, A_, B_)                                                         \
   template <int SIGN, typename C> struct Dft<R_, SIGN, C> {                               \
     static __device__ __forceinline__ void run(C* x) { dft_ab<A_, B_, SIGN, C>(x); }      \
   };
-PAL_COMPOSITE(6, 2, 3)
+#define PAL_PRIME_FACTOR(R_, A_, B_)                                                      \
+  template <int SIGN, typename C> struct Dft<R_, SIGN, C> {                               \
+    static __device__ __forceinline__ void run(C* x) { dft_pfa<A_, B_, SIGN, C>(x); }     \
+  };
+PAL_PRIME_FACTOR(6, 2, 3)
 PAL_COMPOSITE(8, 2, 4)
-PAL_COMPOSITE(12, 3, 4)
+PAL_PRIME_FACTOR(12, 3, 4)
 PAL_COMPOSITE(16, 4, 4)
-PAL_COMPOSITE(24, 3, 8)
+PAL_PRIME_FACTOR(24, 3, 8)
 PAL_COMPOSITE(32, 4, 8)
-PAL_COMPOSITE(48, 3, 16)
+PAL_PRIME_FACTOR(48, 3, 16)
 PAL_COMPOSITE(64, 8, 8)
 #undef PAL_COMPOSITE
+#undef PAL_PRIME_FACTOR
 
 // ---------------------------------------------------------------------------
 // Plan: compile-time radix list for one line length.

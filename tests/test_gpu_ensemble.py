@@ -104,3 +104,22 @@ def test_bad_member_sizes_rejected(ts):
     from palinstrophy_gb300 import _lib as L
     with pytest.raises(L.PalError):
         ts.Ensemble([64, 100], "fp32")
+
+
+def test_sharded_members_equal_the_whole_ensemble(ts):
+    """Members stepped as two rank shards (run one after the other here) give the
+    same fields and scalars, bit for bit, as the same members in one ensemble."""
+    import numpy as np
+    from palinstrophy_gb300.ensemble_shards import gather_rows, run_ensemble_shard
+    Ns = [32, 64, 32, 64, 32]
+    seeds = [11, 12, 13, 14, 15]
+    whole = run_ensemble_shard(Ns, seeds, 0, 1, nsteps=20, update=1, return_fields=True)
+    parts = []
+    for r in range(2):
+        parts.extend(run_ensemble_shard(Ns, seeds, r, 2, nsteps=20, update=1, return_fields=True))
+    parts = gather_rows(parts)  # no process group: rows as they are
+    assert [p["member"] for p in parts] == list(range(len(Ns)))
+    for a, b in zip(whole, parts):
+        for k in ("t", "dt", "cn", "cflm", "it"):
+            assert a[k] == b[k], (a["member"], k)
+        assert np.array_equal(a["om2"], b["om2"])

@@ -213,6 +213,17 @@ int pal_ensemble_get_stream(pal_ensemble* e, void** stream);
 int pal_ensemble_synchronize(pal_ensemble* e);
 int pal_ensemble_last_error(pal_ensemble* e, char* buf, size_t n);
 
+/* PAO / KM3 initial condition generated into the handle (turbo_simulator.py:
+ * 213-485, 1059-1239, 1314-1361): the LCG draws run on the host in the
+ * reference's serial order, the per-mode PAO amplitudes and phases, the KM3
+ * shell sums and rescale, the moments and om2 = i (gamma u1 - alfa u3) on the
+ * device.  Sets om2, the velocity band (as pal_set_velocity_spectrum) and
+ * fnm1 = 0; uc_host, if not null, receives the velocity band (2, N, N/2) in the
+ * handle's precision.  stats[0..2] = Energy, WiWi, visc; *seed_out = final LCG
+ * seed.  Replaces the host-side generator call of create_dns_state.  Waits. */
+int pal_generate(pal_handle* h, double K0, double Re, int seed, int spectrum, void* uc_host, double* stats,
+                 int* seed_out);
+
 /* Host-side PAO / KM3 initial condition (turbo_simulator.py:213-485, 1059-1239,
  * 1314-1361), complex64 outputs: om2 (N, N/2) and uc_low (2, N, N/2).
  * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed. */

@@ -317,6 +317,10 @@ int autotune(pal_handle* h) {
 
 }  // namespace
 
+// Device generator (pal_generate.cu).
+int pal_generate_device(int N, int precision, double K0, double Re, int seed, int spectrum, void* om_dev,
+                        void* uc_dev, cudaStream_t s, double* stats, int* seed_out, std::string* err);
+
 extern "C" {
 
 int pal_supported(int N, int precision) {
@@ -441,6 +445,24 @@ int pal_set_spectral_state(pal_handle* h, const void* om2, const void* fnm1) {
   PAL_CK(h, cudaStreamSynchronize(h->stream));
   h->state = ST_VEL_PENDING;
   h->vel_uploaded = false;
+  return PAL_OK;
+}
+
+int pal_generate(pal_handle* h, double K0, double Re, int seed, int spectrum, void* uc_host, double* stats,
+                 int* seed_out) {
+  if (int rc = check(h)) return rc;
+  if (spectrum != PAL_SPEC_KM3 && spectrum != PAL_SPEC_PAO) return fail(h, PAL_ERR_INVALID, "unknown spectrum");
+  if (!(K0 > 0.0) || !(Re > 0.0)) return fail(h, PAL_ERR_INVALID, "K0 and Re must be positive");
+  std::string err;
+  if (int rc = pal_generate_device(h->N, h->precision, K0, Re, seed, spectrum, h->om, h->stage, h->stream, stats,
+                                   seed_out, &err))
+    return fail(h, rc, err);
+  const size_t bytes = (size_t)h->N * h->Nh * h->esz;
+  PAL_CK(h, cudaMemsetAsync(h->fnm1, 0, bytes, h->stream));
+  if (uc_host) PAL_CK(h, cudaMemcpyAsync(uc_host, h->stage, 2 * bytes, cudaMemcpyDeviceToHost, h->stream));
+  PAL_CK(h, cudaStreamSynchronize(h->stream));
+  h->state = ST_VEL_PENDING;
+  h->vel_uploaded = true;
   return PAL_OK;
 }
 
@@ -850,6 +872,10 @@ int pal_get_field(pal_handle* h, int which, void* host_dst) {
   if (int rc = check(h)) return rc;
   if (!host_dst) return fail(h, PAL_ERR_INVALID, "host_dst is null");
   if (which == PAL_FIELD_OM2 || which == PAL_FIELD_FNM1) {
+    // the stage buffer is the transpose's scratch: a velocity band waiting
+    // there for STEP2A is turned into the U state first
+    if (h->state == ST_VEL_PENDING && h->vel_uploaded)
+      if (int rc = resolve_velocity(h)) return rc;
     h->ks->transpose(which == PAL_FIELD_OM2 ? h->om : h->fnm1, h->stage, h->Nh, h->N, 1, h->stream);
     PAL_LAUNCHED(h, "transpose out");
     PAL_CK(h, cudaMemcpyAsync(host_dst, h->stage, (size_t)h->N * h->Nh * h->esz, cudaMemcpyDeviceToHost, h->stream));

@@ -100,6 +100,17 @@ class Field:
                 raise ValueError(f"uc_low must have shape {(2, self.N, self.N // 2)}")
             self._ck(self.lib.pal_set_velocity_spectrum(self.h, L.ptr(uc)))
 
+    def generate(self, K0: float, Re: float, seed: int, spectrum: str = "KM3"):
+        """PAO / KM3 start generated on the device (pal_generate); returns
+        (uc_low (2, N, N/2) host copy, stats dict as pao_generate's)."""
+        spec = {"KM3": L.PAL_SPEC_KM3, "PAO": L.PAL_SPEC_PAO}[spectrum.upper()]
+        uc = np.empty((2, self.N, self.N // 2), self.cdt)
+        st = (L._D * 3)()
+        so = L.ctypes.c_int(0)
+        self._ck(self.lib.pal_generate(self.h, float(K0), float(Re), int(seed), spec, L.ptr(uc), st,
+                                       L.ctypes.byref(so)))
+        return uc, {"Energy": st[0], "WiWi": st[1], "visc": st[2], "seed_out": so.value}
+
     def set_scalars(self, t=0.0, dt=0.0, cn=1.0, cnm1=0.0, visc=1e-4, cflnum=0.75, it=0):
         self._ck(self.lib.pal_set_scalars(self.h, t, dt, cn, cnm1, visc, cflnum, int(it)))
 
@@ -328,21 +339,29 @@ class DnsState:
 def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float = 0.75,
                      backend: str = "gb300", seed: int = 1, skip_pao: bool = False,
                      populate_compact_ur: bool = True, start_spectrum: SPECTRUM = "KM3",
-                     precision: str = "fp32") -> DnsState:
-    """Allocate the GB300 state and run the PAO/KM3 generator (turbo_simulator.py:878-1054)."""
+                     precision: str = "fp32", generator: str = "device") -> DnsState:
+    """Allocate the GB300 state and run the PAO/KM3 generator (turbo_simulator.py:878-1054):
+    on the device (`generator="device"`, pal_generate) or with the host restatement
+    (`"host"`, pal_pao_generate)."""
     if backend not in ("gb300", "gpu", "auto"):
         raise ValueError(f"backend {backend!r}: this module is the GB300 backend (no CPU path)")
     S = DnsState(N, Re, K0, CFL, seed, start_spectrum, precision, populate_compact_ur)
     if skip_pao:
         return S
-    om2, uc, st = L.pao_generate(N, K0, Re, seed, start_spectrum)
+    if generator == "device":
+        uc, st = S.field.generate(K0, Re, seed, start_spectrum)
+    elif generator == "host":
+        om2, uc, st = L.pao_generate(N, K0, Re, seed, start_spectrum)
+    else:
+        raise ValueError(f"generator {generator!r}: 'device' or 'host'")
     print(f"--- INITIALIZING GB300 --- N={N}, K0={int(K0)}, Re={float(Re):,.1f}, {start_spectrum}")
     print(f" Energy      = {st['Energy']:.8g}")
     print(f" WiWi        = {st['WiWi']:.8g}")
     print(f" Viscosity   = {st['visc']:.8g}")
     print(f" PAO seed in = {seed}")
     print(f" PAO seed out= {st['seed_out']}")
-    S.set_spectral_state(om2, None, uc)
+    if generator == "host":
+        S.set_spectral_state(om2, None, uc)
     S.uc_init = np.asarray(uc, np.complex64)
     S.visc = float(st["visc"])
     S.dt, S.cn, S.cnm1 = 0.0, 1.0, 0.0

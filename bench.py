@@ -421,6 +421,23 @@ def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100
     return {"N8192_fp32": big, "N4096_fp32_vs_fp64_history": drift}
 
 
+def _generator_times(N=N_GRID):
+    """Initial KM3 field at N: the device generator (pal_generate) against the
+    host restatement (pal_pao_generate), wall seconds after one warm-up call."""
+    from palinstrophy_gb300 import _lib as L
+    from palinstrophy_gb300.turbo_simulator import Field
+    F = Field(N, "fp32", RE, CFL)
+    F.generate(K0, RE, SEED, "KM3")
+    t0 = time.perf_counter()
+    F.generate(K0, RE, SEED, "KM3")
+    t_dev = time.perf_counter() - t0
+    F.close()
+    t0 = time.perf_counter()
+    L.pao_generate(N, K0, RE, SEED, "KM3")
+    t_host = time.perf_counter() - t0
+    return {"N": N, "spectrum": "KM3", "device_s": t_dev, "host_s": t_host}
+
+
 def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
     """FP32 CPU port of the reference path: steps/s over a bounded sample."""
     import numpy as np
@@ -514,6 +531,7 @@ def run_gb300(args):
     diff = _differentiation()
     prec_form = _precision_form()
     large = _large_single_field(om2, uc, visc)
+    gen_times = _generator_times()
 
     rate32 = ws * args.steps / (ms32 / 1000.0)
     rate64 = ws * k64 / (ms64 / 1000.0)
@@ -559,6 +577,7 @@ def run_gb300(args):
         "differentiation": diff,
         "precision_form": prec_form,
         "large_single_field": large,
+        "initial_condition": gen_times,
         "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": min(8, os.cpu_count() or 1),
                          "kind": "port",
                          "sample": f"{cpu_n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up ({cpu_s:.1f} s), FP32 "

@@ -904,25 +904,48 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
 
 // om / fnm1 between the natural [kx][z] columns and the butterfly-major
 // columns of the column plan PL (om_p, fm_p; only the N in-band entries of each
-// M-element column are written or read).  One block per kx column.
+// M-element column are written or read).  One block per kx column; the column
+// passes through shared memory, so both the natural and the butterfly-major
+// side are read and written in consecutive order.
 template <typename T, class PL, bool TO_PERM>
 __global__ void __launch_bounds__(256) k_om_perm(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
   constexpr int M = PL::M, N = 2 * M / 3, Nh = M / 3;
+  constexpr int RP = PL::RP, FSTEP = PL::FSTEP;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* so = reinterpret_cast<C*>(smraw);
+  C* sf = so + N;
   const int kx = blockIdx.x;
   C* __restrict__ no = static_cast<C*>(a.om) + (size_t)kx * N;
   C* __restrict__ nf = static_cast<C*>(a.fnm1) + (size_t)kx * N;
   C* __restrict__ po = static_cast<C*>(a.om_p) + (size_t)kx * M;
   C* __restrict__ pf = static_cast<C*>(a.fm_p) + (size_t)kx * M;
-  for (int z = threadIdx.x; z < N; z += 256) {
-    const int p = PL::mid_perm(z < Nh ? z : z + Nh);
-    if constexpr (TO_PERM) {
-      po[p] = no[z];
-      pf[p] = nf[z];
-    } else {
-      no[z] = po[p];
-      nf[z] = pf[p];
+  if constexpr (TO_PERM) {
+    for (int z = threadIdx.x; z < N; z += 256) {
+      so[z] = no[z];
+      sf[z] = nf[z];
+    }
+    __syncthreads();
+  }
+  for (int p = threadIdx.x; p < M; p += 256) {
+    const int f = PL::freq((p % FSTEP) * RP) + (p / FSTEP) * FSTEP;
+    if (f < Nh || f >= N) {
+      const int z = f < Nh ? f : f - Nh;
+      if constexpr (TO_PERM) {
+        po[p] = so[z];
+        pf[p] = sf[z];
+      } else {
+        so[z] = po[p];
+        sf[z] = pf[p];
+      }
+    }
+  }
+  if constexpr (!TO_PERM) {
+    __syncthreads();
+    for (int z = threadIdx.x; z < N; z += 256) {
+      no[z] = so[z];
+      nf[z] = sf[z];
     }
   }
 }

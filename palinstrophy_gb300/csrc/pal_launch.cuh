@@ -135,6 +135,10 @@ struct ColOf {
     e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_inv);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_om_perm<T, PL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_perm);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_om_perm<T, PL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_perm);
+    if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
   static dim3 grid(const StepArgs& a) { return dim3(a.N / 2, a.members > 1 ? a.members : 1); }
@@ -142,8 +146,14 @@ struct ColOf {
   static void col_perm(const StepArgs& a, cudaStream_t s) {
     k_col<T, PL, NT, PERM_PREF, true><<<grid(a), NT, smem_inv, s>>>(a);
   }
-  static void to_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, true><<<grid(a), 256, 0, s>>>(a); }
-  static void from_perm(const StepArgs& a, cudaStream_t s) { k_om_perm<T, PL, false><<<grid(a), 256, 0, s>>>(a); }
+  static constexpr size_t smem_perm = size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>);  // one om + fnm1 column
+  static_assert(smem_perm <= kSmemLimit, "om / fnm1 column does not fit in shared memory");
+  static void to_perm(const StepArgs& a, cudaStream_t s) {
+    k_om_perm<T, PL, true><<<grid(a), 256, smem_perm, s>>>(a);
+  }
+  static void from_perm(const StepArgs& a, cudaStream_t s) {
+    k_om_perm<T, PL, false><<<grid(a), 256, smem_perm, s>>>(a);
+  }
   static void col_inv(const StepArgs& a, cudaStream_t s) {
     k_col_inv<T, PL, NT><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem_inv, s>>>(a);
   }

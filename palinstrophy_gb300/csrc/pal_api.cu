@@ -565,7 +565,11 @@ int pal_step_rk3(pal_handle* h) {
   if (int rc = check(h)) return rc;
   if (int rc = resolve_velocity(h)) return rc;
   if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "LS-IMEX-RK3 step needs the physical velocity");
-  return one_step(h, PAL_LS_IMEX_RK3, false, false);
+  // three column passes: worth the butterfly-major order and its two conversions
+  if (int rc = om_layout(h, true)) return rc;
+  const int rc = one_step(h, PAL_LS_IMEX_RK3, false, false, true);
+  const int rc2 = om_layout(h, false);
+  return rc != PAL_OK ? rc : rc2;
 }
 
 int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update) {

@@ -131,6 +131,26 @@ def _traffic(kernel, prec):
     return None
 
 
+def _limiter(kernel, prec):
+    """What bounds the kernel, from its committed ncu summary (issue and FMA-pipe
+    activity), when one exists."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{prec}_N{N_GRID}.md")
+    issue = fma = None
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("| smsp__issue_active |"):
+                    issue = line.split("|")[2].strip()
+                elif line.startswith("| sm__pipe_fma_cycles_active |"):
+                    fma = line.split("|")[2].strip()
+    except OSError:
+        return None
+    if issue is None:
+        return None
+    return (f"instruction issue and load/store latency, not DRAM bandwidth: ncu issue active {issue}, "
+            f"FP32 FMA pipe {fma} (profiles/{kernel}_{prec}_N{N_GRID}.md)")
+
+
 def _init_arrays():
     from palinstrophy_gb300 import _lib as L
     return L.pao_generate(N_GRID, K0, RE, SEED, "KM3")
@@ -572,6 +592,7 @@ def run_gb300(args):
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(dominant, "fp32"), "algorithmic_bytes": dom_bytes,
                      "ms_per_launch": {"k_row": ms_row, "k_col": ms_col},
+                     "limiter": _limiter(dominant, "fp32"),
                      "stage_bytes_per_s": (bytes_row + bytes_col) / ((ms_row + ms_col) / 1000.0) / 1e9},
         "ensemble": ens,
         "differentiation": diff,

@@ -231,6 +231,34 @@ class Field:
         self._ck(self.lib.pal_field_device_ptr(self.h, which, L.ctypes.byref(p)))
         return p.value
 
+    def device_array(self, which: str):
+        """Zero-copy device view of a field, with __cuda_array_interface__ (v3):
+        "om2" / "fnm1" as the reference's (N, N/2) array (the device keeps them
+        [kx][z], so the view is strided), "u" / "v" as the physical (M, M)
+        planes (materialised first).  Valid until the handle's next call that
+        writes the field; synchronise the handle's stream before reading."""
+        idx = {"om2": L.PAL_FIELD_OM2, "fnm1": L.PAL_FIELD_FNM1, "u": L.PAL_FIELD_UR_U, "v": L.PAL_FIELD_UR_V}[which]
+        if which in ("u", "v"):
+            self._ck(self.lib.pal_materialize_physical(self.h))
+        ptr = self.device_ptr(idx)
+        esz = np.dtype(self.cdt).itemsize
+        if which in ("om2", "fnm1"):
+            N = self.N
+            return _DeviceView(ptr, (N, N // 2), np.dtype(self.cdt).str, (esz, N * esz), self)
+        M = 3 * self.N // 2
+        rsz = esz // 2
+        return _DeviceView(ptr, (M, M), np.dtype(self.cdt).type(0).real.dtype.str, (M * rsz, rsz), self)
+
+
+class _DeviceView:
+    """A device array exposed through __cuda_array_interface__ (version 3); it
+    keeps its handle alive."""
+
+    def __init__(self, ptr, shape, typestr, strides, owner):
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "strides": tuple(strides), "version": 3, "stream": None}
+
 
 class DnsState:
     """GB300 twin of the reference DnsState (turbo_simulator.py:654-810).
@@ -296,6 +324,15 @@ class DnsState:
     @property
     def fnm1(self):
         return self._field.fnm1()
+
+    @property
+    def om2_device(self):
+        """om2 as a zero-copy device view (reference shape (N, N/2), strided)."""
+        return self._field.device_array("om2")
+
+    def ur_device(self, comp: int):
+        """Physical velocity component 0 (u) or 1 (v) as a zero-copy (M, M) device view."""
+        return self._field.device_array("u" if comp == 0 else "v")
 
     @property
     def ur_full(self):

@@ -401,3 +401,27 @@ def test_k4_start_runs(ts):
     F.step("LS_IMEX_RK3", 5, update=1, final_update=True)
     assert F.diagnostics()["nonfinite"] == 0
     F.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_device_views_match_host_copies(ts, prec):
+    """__cuda_array_interface__ views of om2 / fnm1 (strided: the device keeps them
+    [kx][z]) and of the physical u, v planes read the same values as the copies."""
+    import torch
+    from palinstrophy_gb300 import _lib as L
+    om2, uc, st = L.pao_generate(64, 10.0, 1e4, 4895, "KM3")
+    F = ts.Field(64, prec, 1e4, 0.5)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", st["visc"])
+    F.step2a()
+    F.set_scalar("dt", 1e-3)
+    F.step("CNAB2", 3, update=0)
+    F.synchronize()
+    for name, host in (("om2", F.om2()), ("fnm1", F.fnm1())):
+        t = torch.as_tensor(F.device_array(name), device="cuda")
+        assert t.shape == host.shape
+        assert np.array_equal(t.cpu().numpy(), host)
+    u = torch.as_tensor(F.device_array("u"), device="cuda")
+    F.synchronize()
+    assert np.array_equal(u.cpu().numpy(), F.ur(0))
+    F.close()

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in ``palinstrophy_gb300`` imports this
 module; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
-of ``bench.py`` may use it, as the checker of the product's own generator.
+of ``bench.py`` may use it, to check the product's own generator against it.
 
 It follows the reference generator step by step so that, on the same machine,
 it reproduces the reference arrays:

@@ -19,7 +19,7 @@ Same variable names, dimension names, shapes and attribute names:
 
 Container: the reference writes NETCDF4 (an HDF5 file, zlib level 4 with
 shuffle) through the netCDF4 package.  Neither netCDF4 nor an HDF5 library is
-part of this build, so files are written in the netCDF classic 64-bit-offset
+a dependency of this package, so files are written in the netCDF classic 64-bit-offset
 format (CDF-2) with scipy.io.netcdf_file: the netCDF library opens classic and
 NETCDF4 files through the same Dataset call, so the reference's loader reads
 these files unchanged.  Reading a NETCDF4/HDF5 file written by the reference

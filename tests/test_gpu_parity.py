@@ -425,3 +425,42 @@ def test_device_views_match_host_copies(ts, prec):
     F.synchronize()
     assert np.array_equal(u.cpu().numpy(), F.ur(0))
     F.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 1e-4)])
+def test_precision_form_config_n1024(ts, prec, tol):
+    """The precision-form configuration at its own size: N=1024 from the labelled
+    k^4 unit-energy start (K0=15, seed 4895), Re=1e4, LS-IMEX-RK3 at CFL 0.1,
+    NEXTDT every 10 steps; 20 steps against the FP64 oracle."""
+    from palinstrophy_gb300.initial import k4_unit_energy
+    N, cfl, steps, update = 1024, 0.1, 20, 10
+    om2, uc = k4_unit_energy(N, 15.0, 4895)
+    visc = float(np.float32(1.0 / np.float32(1e4)))
+    F, S = _pair(ts, N, prec, om2, uc, visc, cfl)
+    _gpu_init_dt(F)
+    do.init_dt(S)
+    do.run(S, steps, "LS_IMEX_RK3", update)
+    F.step("LS_IMEX_RK3", steps, update=update, final_update=True)
+    err = do.rel_l2(S.om2, F.om2())
+    assert err <= tol, err
+    assert abs(F.scalars()["dt"] - S.dt) <= (1e-13 if prec == "fp64" else 1e-5) * S.dt
+    F.close()
+
+
+def test_reference_plain_config_blows_up_like_the_reference(ts):
+    """The plain CPU configuration (N=256 KM3 K0=10 seed 4895, Re=1e4, CNAB2,
+    CFL 0.75, NEXTDT every 100 steps) is unstable: the reference's own run_dns
+    turns non-finite between steps 200 and 300 (ITERATION 300 prints DT=nan).
+    The FP64 path follows the oracle up to step 200 and then turns non-finite
+    with it, and the diagnostics flag it."""
+    om2, uc, visc = _init("init_KM3_N256_s4895_k10.npz")
+    for steps, finite in ((200, True), (300, False)):
+        F, S, _, _, _ = _run_pair(ts, 256, "fp64", "init_KM3_N256_s4895_k10.npz", 0.75, "CNAB2", steps, 100)
+        if finite:
+            assert np.isfinite(S.om2).all()
+            assert do.rel_l2(S.om2, F.om2()) <= 1e-9
+        else:
+            assert not np.isfinite(S.om2).all()
+            assert not np.isfinite(F.om2()).all()
+            assert F.diagnostics()["nonfinite"] != 0
+        F.close()

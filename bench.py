@@ -237,6 +237,7 @@ def _ensemble_rate(steps=1000, warmup=20):
     from palinstrophy_gb300.turbo_simulator import Ensemble
     Ns = [256] * 32 + [384] * 32 + [512] * 32
     E = Ensemble(Ns, "fp32", 1e4, 0.5)
+    E.autotune()  # candidates timed on the batched launch shape of each size group
     for m, n in enumerate(Ns):
         om2, uc, st = L.pao_generate(n, 10.0, 1e4, m + 1, "KM3")
         E.set_member(m, om2, None, uc)
@@ -254,11 +255,12 @@ def _ensemble_rate(steps=1000, warmup=20):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     dts = sorted(E.scalars(m)["dt"] for m in (0, 40, 95))
+    variants = {n: E.variant(n) for n in (256, 384, 512)}
     E.close()
     return {"members": len(Ns), "sizes": [256, 384, 512], "steps": steps,
             "ensemble_steps_per_s": steps / (ms / 1000.0),
             "member_steps_per_s": len(Ns) * steps / (ms / 1000.0),
-            "launches_per_step": 6, "cuda_graph": True, "sample_member_dt": dts}
+            "launches_per_step": 6, "cuda_graph": True, "sample_member_dt": dts, "kernels": variants}
 
 
 def _differentiation(directions=8):

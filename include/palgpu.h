@@ -206,6 +206,13 @@ int pal_ensemble_init_dt(pal_ensemble* e);
  * it % update == 0 or it == 1 (update > 0); use_graph captures the launch
  * sequence once per pattern and replays it. */
 int pal_ensemble_step(pal_ensemble* e, int method, int nsteps, int update, int use_graph);
+/* Re-tune each group's row / column candidates on its batched launch shape;
+ * call right after pal_ensemble_create, before any member is set.  Without it
+ * the groups use the single-field choice of pal_create (members then match
+ * single fields bit for bit; tuned groups match them to rounding). */
+int pal_ensemble_autotune(pal_ensemble* e);
+/* Candidates of the group of size group_N, as "row[...] col[...]". */
+int pal_ensemble_get_variant(pal_ensemble* e, int group_N, char* desc, size_t desc_len);
 int pal_ensemble_get_member(pal_ensemble* e, int member, int which, void* host_dst);
 int pal_ensemble_get_scalars(pal_ensemble* e, int member, double* t, double* dt, double* cn, double* cflm,
                              long long* it);

@@ -51,6 +51,8 @@ _SIGS = {
     "pal_destroy": (_I, [_H]),
     "pal_supported": (_I, [_I, _I]),
     "pal_generate": (_I, [_H, _D, _D, _I, _I, _P, ctypes.POINTER(_D), ctypes.POINTER(_I)]),
+    "pal_ensemble_autotune": (_I, [_H]),
+    "pal_ensemble_get_variant": (_I, [_H, _I, ctypes.c_char_p, ctypes.c_size_t]),
     "pal_device_info": (_I, [ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.c_char_p, ctypes.c_size_t]),
     "pal_set_spectral_state": (_I, [_H, _P, _P]),
     "pal_set_velocity_spectrum": (_I, [_H, _P]),

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -71,6 +72,7 @@ struct pal_ensemble {
   std::map<std::string, cudaGraphExec_t> graphs;
   long long it = 0;
   bool ready = false;  // velocities resolved, dt initialised
+  bool has_members = false;  // a member has been set (the buffers hold state)
   std::string err;
 };
 
@@ -225,8 +227,11 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
     const size_t plane_w = (size_t)g.Nh * g.M * e->esz, plane_om = (size_t)g.Nh * g.N * e->esz;
     g.part_stride = std::max<long long>(2LL * g.M, 5 * 1024);
     void** bufs[] = {&g.w0, &g.w1, &g.om, &g.fnm1, &g.vel, &g.tw_row, &g.tw_col, &g.om_p};
+    size_t tw_row_max = 0, tw_col_max = 0;  // room for any candidate's tables (pal_ensemble_autotune)
+    for (int q = 0; q < g.ks->n_rows; ++q) tw_row_max = std::max(tw_row_max, (size_t)g.ks->rows[q].tw_elems);
+    for (int q = 0; q < g.ks->n_cols; ++q) tw_col_max = std::max(tw_col_max, (size_t)g.ks->cols[q].tw_elems);
     const size_t sizes[] = {nm * plane_w, nm * plane_w, nm * plane_om, nm * plane_om, 2 * nm * plane_om,
-                            (size_t)g.rk->tw_elems * e->esz, (size_t)g.ck->tw_elems * e->esz, 2 * nm * plane_w};
+                            tw_row_max * e->esz, tw_col_max * e->esz, 2 * nm * plane_w};
     for (int i = 0; i < 8; ++i) {
       c = cudaMalloc(bufs[i], sizes[i]);
       if (c == cudaSuccess) c = cudaMemsetAsync(*bufs[i], 0, sizes[i], e->stream);
@@ -302,7 +307,101 @@ int pal_ensemble_set_member(pal_ensemble* e, int member, const void* om2, const 
   g.has_vel[loc] = uc_low != nullptr;
   ENS_CK(e, cudaStreamSynchronize(e->stream));
   e->ready = false;
+  e->has_members = true;
   return PAL_OK;
+}
+
+// Time every row and column candidate on each group's batched launch shape
+// (grid.y = members) and keep the fastest; the buffers still hold zeros, so
+// the timing launches disturb no state.  Without it the groups use the
+// candidates pal_create tuned for a single field of the same size, which
+// keeps ensemble members bit-identical to single fields.
+int pal_ensemble_autotune(pal_ensemble* e) {
+  if (!e) return efail(nullptr, PAL_ERR_INVALID, "null ensemble");
+  if (e->has_members) return efail(e, PAL_ERR_STATE, "autotune before setting members");
+  const char* env = std::getenv("PAL_AUTOTUNE");
+  if (env && env[0] == '0') return PAL_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ENS_CK(e, cudaEventCreate(&e0));
+  ENS_CK(e, cudaEventCreate(&e1));
+  auto time_it = [&](auto&& launch) -> float {
+    launch();  // warm-up
+    cudaEventRecord(e0, e->stream);
+    for (int q = 0; q < 3; ++q) launch();
+    cudaEventRecord(e1, e->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  int rc = PAL_OK;
+  for (Group& g : e->groups) {
+    const int nm = (int)g.members.size();
+    float best = 1e30f;
+    const pal::RowKernels* best_r = g.rk;
+    for (int q = 0; q < g.ks->n_rows && rc == PAL_OK; ++q) {
+      const pal::RowKernels* rk = &g.ks->rows[q];
+      if (rk->configure() != cudaSuccess) continue;
+      if (rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, rk->V, nm)) continue;
+      rk->twiddles(g.tw_row, e->stream);
+      StepArgs a = group_args(e, g);
+      const float ms = time_it([&]() { rk->row(a, e->stream); });
+      if (cudaGetLastError() != cudaSuccess) rc = efail(e, PAL_ERR_CUDA, "ensemble autotune (row)");
+      if (ms < best) {
+        best = ms;
+        best_r = rk;
+      }
+    }
+    best = 1e30f;
+    const pal::ColKernels* best_c = g.ck;
+    for (int q = 0; q < g.ks->n_cols && rc == PAL_OK; ++q) {
+      const pal::ColKernels* ck = &g.ks->cols[q];
+      if (ck->configure() != cudaSuccess) continue;
+      ck->twiddles(g.tw_col, e->stream);
+      StepArgs a = group_args(e, g);
+      a.tw = g.tw_col;
+      a.scheme = 0;
+      const float ms = time_it([&]() { ck->col_perm(a, e->stream); });
+      if (cudaGetLastError() != cudaSuccess) rc = efail(e, PAL_ERR_CUDA, "ensemble autotune (column)");
+      if (ms < best) {
+        best = ms;
+        best_c = ck;
+      }
+    }
+    if (rc != PAL_OK) break;
+    g.rk = best_r;
+    g.ck = best_c;
+    if (g.rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, g.rk->V, nm)) {
+      rc = efail(e, PAL_ERR_CUDA, "ensemble TMA descriptors");
+      break;
+    }
+    g.rk->twiddles(g.tw_row, e->stream);
+    g.ck->twiddles(g.tw_col, e->stream);
+    const size_t plane_w = (size_t)g.Nh * g.M * e->esz, plane_om = (size_t)g.Nh * g.N * e->esz;
+    cudaMemsetAsync(g.w0, 0, nm * plane_w, e->stream);
+    cudaMemsetAsync(g.w1, 0, nm * plane_w, e->stream);
+    cudaMemsetAsync(g.om, 0, nm * plane_om, e->stream);
+    cudaMemsetAsync(g.fnm1, 0, nm * plane_om, e->stream);
+    cudaMemsetAsync(g.om_p, 0, 2 * nm * plane_w, e->stream);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
+  e->graphs.clear();
+  if (rc != PAL_OK) return rc;
+  ENS_CK(e, cudaStreamSynchronize(e->stream));
+  return PAL_OK;
+}
+
+int pal_ensemble_get_variant(pal_ensemble* e, int group_N, char* desc, size_t desc_len) {
+  if (!e || !desc || !desc_len) return efail(e, PAL_ERR_INVALID, "bad arguments");
+  for (const Group& g : e->groups) {
+    if (g.N == group_N) {
+      std::snprintf(desc, desc_len, "row[%s] col[%s]", g.rk->name, g.ck->name);
+      return PAL_OK;
+    }
+  }
+  return efail(e, PAL_ERR_INVALID, "no group of that size");
 }
 
 int pal_ensemble_set_scalar(pal_ensemble* e, int member, int which, double value) {

@@ -587,6 +587,15 @@ class Ensemble:
         except Exception:
             pass
 
+    def autotune(self):
+        """Re-tune each size group on its batched shape (before any member is set)."""
+        self._ck(self.lib.pal_ensemble_autotune(self.h))
+
+    def variant(self, N: int) -> str:
+        buf = L.ctypes.create_string_buffer(256)
+        self._ck(self.lib.pal_ensemble_get_variant(self.h, int(N), buf, len(buf)))
+        return buf.value.decode()
+
     def set_member(self, m, om2, fnm1=None, uc_low=None):
         om2 = np.ascontiguousarray(om2, dtype=self.cdt)
         f = None if fnm1 is None else np.ascontiguousarray(fnm1, dtype=self.cdt)

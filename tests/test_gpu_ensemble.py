@@ -123,3 +123,36 @@ def test_sharded_members_equal_the_whole_ensemble(ts):
         for k in ("t", "dt", "cn", "cflm", "it"):
             assert a[k] == b[k], (a["member"], k)
         assert np.array_equal(a["om2"], b["om2"])
+
+
+def test_batched_autotune(ts):
+    """Groups re-tuned on their batched shape still give the single-field results
+    to rounding; tuning after a member is set is refused."""
+    import numpy as np
+    from palinstrophy_gb300 import _lib as L
+    Ns = [64] * 4 + [128] * 3
+    E = ts.Ensemble(Ns, "fp32", 1e4, 0.5)
+    E.autotune()
+    assert E.variant(64).startswith("row[") and E.variant(128).startswith("row[")
+    inits = []
+    for m, n in enumerate(Ns):
+        om2, uc, st = L.pao_generate(n, 10.0, 1e4, m + 1, "KM3")
+        inits.append((om2, uc, st))
+        E.set_member(m, om2, None, uc)
+        E.set_scalar(m, "visc", st["visc"])
+    with pytest.raises(ts.L.PalError if hasattr(ts, "L") else Exception):
+        E.autotune()
+    E.init_dt()
+    E.step("CNAB2", 10, update=1)
+    for m in (0, 5):
+        om2, uc, st = inits[m]
+        F = ts.Field(Ns[m], "fp32", 1e4, 0.5)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.step2a()
+        F.set_scalar("dt", 0.5 / (F.compute_cflm() * np.pi))
+        F.step("CNAB2", 10, update=1)
+        a, b = E.om2(m).astype(np.complex128), F.om2().astype(np.complex128)
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
+        F.close()
+    E.close()

@@ -1,4 +1,4 @@
-// FP32 candidates, N = 32 .. 768 (M = 48 .. 1152).  The last radix is the
+// FP32 candidates, N = 32 .. 256 (M = 48 .. 384).  The last radix is the
 // fused middle pass and must be even.
 #include "pal_launch.cuh"
 
@@ -10,12 +10,6 @@ using P96 = Plan<96, 16, 6>;
 using P192 = Plan<192, 16, 12>;
 using P384 = Plan<384, 16, 24>;
 using P384b = Plan<384, 24, 16>;
-using P576 = Plan<576, 24, 24>;
-using P576b = Plan<576, 6, 6, 16>;
-using P768 = Plan<768, 32, 24>;
-using P768b = Plan<768, 16, 2, 24>;
-using P1152 = Plan<1152, 8, 6, 24>;
-using P1152b = Plan<1152, 12, 4, 24>;
 
 const RowKernels r32[] = {RowOf<float, P48, 4, 64>::make("8.6 V4x64"), RowOf<float, P48, 2, 64>::make("8.6 V2x64")};
 const ColKernels c32[] = {ColOf<float, P48, 64>::make("8.6 x64")};
@@ -26,31 +20,17 @@ const RowKernels r128[] = {RowOf<float, P192, 4, 128>::make("16.12 V4x128"),
 const ColKernels c128[] = {ColOf<float, P192, 64>::make("16.12 x64"), ColOf<float, P192, 128>::make("16.12 x128")};
 const RowKernels r256[] = {RowOf<float, P384, 4, 256>::make("16.24 V4x256"),
                            RowOf<float, P384, 2, 128>::make("16.24 V2x128"),
-                           RowOf<float, P384b, 4, 256>::make("24.16 V4x256")};
+                           RowOf<float, P384b, 4, 256>::make("24.16 V4x256"),
+                           RowOf<float, Rec<P384>, 4, 256, 2>::make("16.24r V4x256 paired"),
+                           RowOf<float, Rec<P384b>, 4, 256, 2>::make("24.16r V4x256 paired")};
 const ColKernels c256[] = {ColOf<float, P384, 128>::make("16.24 x128"), ColOf<float, P384, 64>::make("16.24 x64"),
-                           ColOf<float, P384b, 128>::make("24.16 x128")};
-const RowKernels r384[] = {RowOf<float, P576, 4, 256>::make("24.24 V4x256"),
-                           RowOf<float, P576, 2, 128>::make("24.24 V2x128"),
-                           RowOf<float, P576b, 4, 256>::make("6.6.16 V4x256")};
-const ColKernels c384[] = {ColOf<float, P576, 128>::make("24.24 x128"), ColOf<float, P576b, 128>::make("6.6.16 x128")};
-const RowKernels r512[] = {RowOf<float, P768, 4, 256>::make("32.24 V4x256"),
-                           RowOf<float, P768, 2, 128>::make("32.24 V2x128"),
-                           RowOf<float, P768b, 4, 256>::make("16.2.24 V4x256")};
-const ColKernels c512[] = {ColOf<float, P768, 128>::make("32.24 x128"), ColOf<float, P768b, 128>::make("16.2.24 x128"),
-                           ColOf<float, P768, 256>::make("32.24 x256")};
-const RowKernels r768[] = {RowOf<float, P1152, 4, 256>::make("8.6.24 V4x256"),
-                           RowOf<float, P1152, 2, 256>::make("8.6.24 V2x256"),
-                           RowOf<float, P1152b, 4, 256>::make("12.4.24 V4x256")};
-const ColKernels c768[] = {ColOf<float, P1152, 256>::make("8.6.24 x256"), ColOf<float, P1152, 128>::make("8.6.24 x128"),
-                           ColOf<float, P1152b, 256>::make("12.4.24 x256")};
-
+                           ColOf<float, P384b, 128>::make("24.16 x128"),
+                           ColOf<float, Rec<P384>, 128, 2>::make("16.24r x128 hoist"),
+                           ColOf<float, Rec<P384b>, 128, 2>::make("24.16r x128 hoist")};
 PAL_KERNEL_SET_ADJ(float, 0, 32, r32, c32, (AdjOf<float, P48, 4, 64, P48, 64>::get()))
 PAL_KERNEL_SET_ADJ(float, 0, 64, r64, c64, (AdjOf<float, P96, 4, 128, P96, 64>::get()))
 PAL_KERNEL_SET_ADJ(float, 0, 128, r128, c128, (AdjOf<float, P192, 4, 128, P192, 64>::get()))
 PAL_KERNEL_SET_ADJ(float, 0, 256, r256, c256, (AdjOf<float, P384, 4, 256, P384, 128>::get()))
-PAL_KERNEL_SET(float, 0, 384, r384, c384)
-PAL_KERNEL_SET_ADJ(float, 0, 512, r512, c512, (AdjOf<float, P768, 4, 256, P768, 128>::get()))
-PAL_KERNEL_SET(float, 0, 768, r768, c768)
 }  // namespace
 
 const KernelSet* pal_kernels_f32_a(int N) {
@@ -59,9 +39,6 @@ const KernelSet* pal_kernels_f32_a(int N) {
     case 64: return &kSet64;
     case 128: return &kSet128;
     case 256: return &kSet256;
-    case 384: return &kSet384;
-    case 512: return &kSet512;
-    case 768: return &kSet768;
     default: return nullptr;
   }
 }

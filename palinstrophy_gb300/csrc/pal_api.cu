@@ -49,6 +49,7 @@ struct pal_handle {
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
   void *om_p = nullptr, *fm_p = nullptr;  // om / fnm1 in butterfly-major order, used inside pal_step
   pal::TmaMaps tmaps{};                   // w0 / w1 descriptors when the row candidate stores through TMA
+  std::map<std::string, cudaGraphExec_t> step_graphs;  // pal_step sequences of small grids, by NEXTDT pattern
   void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
   void *vis_w = nullptr;      // two scratch work planes for display transforms
@@ -233,6 +234,8 @@ int select_variant(pal_handle* h, int row, int col) {
     return fail(h, PAL_ERR_INVALID, "variant index out of range");
   h->row_idx = row;
   h->col_idx = col;
+  for (auto& kv : h->step_graphs) cudaGraphExecDestroy(kv.second);  // they hold the old kernels
+  h->step_graphs.clear();
   h->rk = &h->ks->rows[row];
   h->ck = &h->ks->cols[col];
   if (h->rk->tma && !pal::encode_row_maps(&h->tmaps, h->w0, h->w1, h->N, h->rk->V, 1))
@@ -418,6 +421,8 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
 int pal_destroy(pal_handle* h) {
   if (!h) return PAL_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& kv : h->step_graphs) cudaGraphExecDestroy(kv.second);
+  h->step_graphs.clear();
   void* bufs[] = {h->w0,     h->w1,   h->om,   h->fnm1, h->stage, h->tw_row,   h->tw_col,
                   h->phys,   h->sc,   h->part, h->vis_w, h->vis_phys, h->om_p};
   for (void* b : bufs)
@@ -572,6 +577,11 @@ int pal_step_rk3(pal_handle* h) {
   return rc != PAL_OK ? rc : rc2;
 }
 
+// Grids up to this size are launch-bound: their step sequences are captured
+// once per NEXTDT pattern and replayed as CUDA graphs.
+constexpr int kStepGraphMaxN = 1024;
+constexpr size_t kStepGraphCache = 16;
+
 int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update) {
   if (int rc = check(h)) return rc;
   if (method != PAL_CNAB2 && method != PAL_LS_IMEX_RK3) return fail(h, PAL_ERR_INVALID, "unknown time stepper");
@@ -580,22 +590,56 @@ int pal_step(pal_handle* h, int method, int nsteps, int update, int final_update
   if (h->state != ST_U) return fail(h, PAL_ERR_STATE, "pal_step needs the physical velocity");
   bool pending = false;
   if (nsteps > 0) {
-    // the butterfly-major om order pays for its two conversions (~60 us each at
-    // N=4096) within one step: three natural-order column passes cost ~370 us more
-    const bool perm = true;
-    if (perm)
-      if (int rc = om_layout(h, true)) return rc;
-    int rc = PAL_OK;
-    for (int j = 1; j <= nsteps && rc == PAL_OK; ++j) {
-      const long long it = h->it + 1;
-      rc = one_step(h, method, pending, true, perm);
-      if (rc != PAL_OK) break;
-      h->it = it;
+    // fused NEXTDT at the start of step j when the previous step ended on the cadence
+    std::string key = std::to_string(method) + ":";
+    std::vector<char> upd(nsteps);
+    const long long it0 = h->it;
+    for (int j = 1; j <= nsteps; ++j) {
+      upd[j - 1] = pending;
+      key += pending ? '1' : '0';
+      const long long it = it0 + j;
       pending = update > 0 && (it % update == 0 || it == 1 || (final_update && j == nsteps));
     }
-    const int rc2 = perm ? om_layout(h, false) : PAL_OK;
-    if (rc != PAL_OK) return rc;
-    if (rc2 != PAL_OK) return rc2;
+    // The column pass runs on the butterfly-major om order, whose two
+    // conversions (~60 us each at N=4096) cost less than one step's three
+    // natural-order column passes (~370 us more).
+    auto record = [&]() -> int {
+      if (int rc = om_layout(h, true)) return rc;
+      int rc = PAL_OK;
+      for (int j = 0; j < nsteps && rc == PAL_OK; ++j) rc = one_step(h, method, upd[j] != 0, true, true);
+      const int rc2 = om_layout(h, false);
+      return rc != PAL_OK ? rc : rc2;
+    };
+    const char* env = std::getenv("PAL_STEP_GRAPHS");
+    const bool graphs = h->N <= kStepGraphMaxN && nsteps >= 2 && !(env && env[0] == '0');
+    if (!graphs) {
+      if (int rc = record()) return rc;
+    } else {
+      auto found = h->step_graphs.find(key);
+      if (found == h->step_graphs.end()) {
+        if (h->step_graphs.size() >= kStepGraphCache) {
+          for (auto& kv : h->step_graphs) cudaGraphExecDestroy(kv.second);
+          h->step_graphs.clear();
+        }
+        PAL_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = record();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        if (rc != PAL_OK) {
+          if (graph) cudaGraphDestroy(graph);
+          return rc;
+        }
+        if (ce != cudaSuccess) return cuda_fail(h, ce, "step graph capture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(h, ie, "step graph instantiate");
+        found = h->step_graphs.emplace(key, exec).first;
+      }
+      PAL_CK(h, cudaGraphLaunch(found->second, h->stream));
+      h->state = ST_U;
+    }
+    h->it = it0 + nsteps;
   }
   if (pending) return launch_phys(h, pal::F_UPDATE_DT);
   return PAL_OK;

@@ -464,3 +464,25 @@ def test_reference_plain_config_blows_up_like_the_reference(ts):
             assert not np.isfinite(F.om2()).all()
             assert F.diagnostics()["nonfinite"] != 0
         F.close()
+
+
+@pytest.mark.parametrize("method", ["CNAB2", "LS_IMEX_RK3"])
+def test_step_graph_replay_equals_direct_launches(ts, method, monkeypatch):
+    """Small grids replay pal_step sequences from CUDA graphs (one per NEXTDT
+    pattern); the replayed steps equal directly launched ones bit for bit."""
+    from palinstrophy_gb300 import _lib as L
+    om2, uc, st = L.pao_generate(128, 12.0, 1e4, 4895, "KM3")
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("PAL_STEP_GRAPHS", mode)
+        F = ts.Field(128, "fp32", 1e4, 0.5)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        _gpu_init_dt(F)
+        for _ in range(3):  # the same pattern three times: captured once, replayed twice
+            F.step(method, 10, update=5)
+        out[mode] = (F.om2(), F.scalars())
+        F.close()
+    assert np.array_equal(out["1"][0], out["0"][0])
+    for k in ("t", "dt", "cn", "cnm1", "it"):
+        assert out["1"][1][k] == out["0"][1][k], k

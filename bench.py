@@ -618,14 +618,24 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
                     help="profiling target: init + 2 warm-up + 2 timed steps of one precision, no JSON")
+    ap.add_argument("--ncu-n", type=int, default=N_GRID,
+                    help="grid size of --ncu-case (4096 or 8192 FP32 / 4096 FP64), device generator start")
     ap.add_argument("--variant", default=None,
                     help="row,col kernel candidates for --ncu-case (skips the autotuning launches)")
     args = ap.parse_args()
     if args.ncu_case:
         if args.variant:
             os.environ["PAL_AUTOTUNE"] = "0"
-        om2, uc, st = _init_arrays()
-        F = _field(args.ncu_case, om2, uc, st["visc"])
+        if args.ncu_n != N_GRID:
+            from palinstrophy_gb300.turbo_simulator import Field
+            F = Field(args.ncu_n, args.ncu_case, RE, CFL)
+            _, st = F.generate(K0, RE, SEED, "KM3")
+            F.set_scalar("visc", st["visc"])
+            F.step2a()
+            F.set_scalar("dt", CFL / (F.compute_cflm() * math.pi))
+        else:
+            om2, uc, st = _init_arrays()
+            F = _field(args.ncu_case, om2, uc, st["visc"])
         if args.variant:
             r, c = (int(x) for x in args.variant.split(","))
             F.set_variant(r, c)

@@ -74,7 +74,7 @@ struct StepArgs {
 // TMA descriptors of the two work planes, each a 3D view (2M floats, N/2 rows,
 // members) with a (2V floats, 256 rows, 1) box: one box is 256 rows of one row
 // tile.  Passed to the row kernel as a __grid_constant__ parameter.
-struct alignas(64) TmaMaps {
+struct TmaMaps {  // aligned as CUtensorMap
   CUtensorMap w0, w1;
 };
 

@@ -1,0 +1,53 @@
+"""bench.py's host-side helpers (no GPU): the roofline fields it reads from the
+committed ncu summaries, and the reference arm's JSON line shape."""
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_traffic_and_limiter_come_from_the_profiles(bench):
+    t_row = bench._traffic("k_row", "fp32")
+    t_col = bench._traffic("k_col", "fp32")
+    assert t_row is not None and 3.0e8 < t_row < 5.0e8  # ~0.35 GB per N=4096 launch
+    assert t_col is not None and 5.0e8 < t_col < 8.0e8
+    lim = bench._limiter("k_row", "fp32")
+    assert lim and "issue" in lim and "profiles/k_row_fp32_N4096.md" in lim
+    assert bench._traffic("k_nonexistent", "fp32") is None
+
+
+def test_rel_l2(bench):
+    import numpy as np
+    a = np.ones(4, np.complex64)
+    assert bench._rel_l2(a, a) == 0.0
+    assert abs(bench._rel_l2(2 * a, a) - 1.0) < 1e-12
+
+
+def test_reference_arm_rank_nonzero_prints_nothing():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1"],
+                         env=env, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0
+    assert out.stdout.strip() == ""
+
+
+def test_warmup_is_raised_to_three(bench, monkeypatch, capsys):
+    """The timing contract needs at least 3 warm-up steps; smaller values are raised."""
+    seen = {}
+    monkeypatch.setattr(bench, "run_reference", lambda args: seen.setdefault("warmup", args.warmup))
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--warmup", "1"])
+    bench.main()
+    assert seen["warmup"] == 3

@@ -194,6 +194,15 @@ int launch_phys(pal_handle* h, int flags) {
 int read_scalars(pal_handle* h) {
   PAL_CK(h, cudaMemcpyAsync(h->sc_host, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->stream));
   PAL_CK(h, cudaStreamSynchronize(h->stream));
+  if (h->sc_host->wait_timeout) {
+    // a kernel gave up waiting for its own bulk copies; clear the flag and report
+    const int zero = 0;
+    cudaMemcpyAsync(reinterpret_cast<char*>(h->sc) + offsetof(DevScalars, wait_timeout), &zero, sizeof(int),
+                    cudaMemcpyHostToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    h->sc_host->wait_timeout = 0;
+    return fail(h, PAL_ERR_CUDA, "a device wait for bulk copies timed out; the last steps are not valid");
+  }
   return PAL_OK;
 }
 

@@ -13,6 +13,8 @@ const RowKernels r4096[] = {RowOf<float, P6144, 4, 512>::make("16.16.24 V4x512")
                             RowOf<float, Rec<P6144>, 4, 512, 3>::make("16.16.24r V4x512 paired l2pf"),
                             RowOf<float, Rec<P6144>, 4, 768, 3>::make("16.16.24r V4x768 paired l2pf"),
                             RowOf<float, Rec<P6144>, 4, 768, 7>::make("16.16.24r V4x768 paired l2pf tma"),
+                            RowOf<float, Rec<P6144>, 4, 768, 11>::make("16.16.24r V4x768 tma-in l2pf"),
+                            RowOf<float, Rec<P6144>, 4, 768, 15>::make("16.16.24r V4x768 tma-in tma-out l2pf"),
                             RowOf<float, Rec<P6144>, 4, 1024, 3>::make("16.16.24r V4x1024 paired l2pf"),
                             RowOf<float, Rec<P6144b>, 4, 512, 2>::make("32.8.24r V4x512 paired")};
 const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),

@@ -39,7 +39,7 @@ struct DevScalars {
   double E, L, Z, P, kmax2;
   long long it;
   int nonfinite;
-  int pad_;
+  int wait_timeout;  // set by a kernel whose bounded wait for its own bulk copies ran out
   unsigned int row_counter, col_counter, diag_counter, phys_counter;
 };
 
@@ -241,6 +241,51 @@ __device__ __forceinline__ void row_first_pass(const StepArgs& a, cplx<T>* sm, i
   __syncthreads();
 }
 
+// Bulk tensor stores (TMA) from shared memory.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int x, int y, int z) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map), "r"(s),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void tma_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Bulk tensor loads (TMA) into shared memory, completed on an mbarrier.
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(const CUtensorMap* map, void* smem, unsigned long long* bar, int x, int y,
+                                            int z) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(d),
+      "l"(map), "r"(b), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+// Wait for phase `parity` of the mbarrier, giving up after max_iter polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int max_iter) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  for (int i = 0; i < max_iter; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // First inverse DIF pass with each U-state row read once.  Butterfly i holds
 // z[i + j S]; the mirrored entry z[M - k] = conj(u^[k]) + i conj(v^[k]) of a
 // row k = i + j S < N/2 sits in butterfly S - i at index R-1-j.  Butterflies 0
@@ -317,6 +362,94 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
   __syncthreads();
 }
 
+// The paired first pass with its U-state rows brought in by the TMA unit: one
+// elected thread issues 3D bulk tensor loads of the tile's rows below N/2
+// (256-row boxes of both planes) into the tile region, laid out [plane][k][v];
+// every thread reads its item's rows from there into registers, a barrier
+// frees the region, and the DFTs write the tile as in row_first_pass_paired.
+// No thread spends load instructions or LSU queue entries on global memory.
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* sm, int z0, int tid,
+                                                   const TmaMaps& maps, unsigned long long* bar) {
+  using C = cplx<T>;
+  constexpr int M = PL::M;
+  constexpr int R = PL::R[0];
+  constexpr int S = M / R;
+  constexpr int SP = PL::pstride(0);
+  constexpr int Nh = M / 3;
+  constexpr int NQ = S / 2;
+  constexpr int BOX = 256;
+  static_assert(sizeof(C) == 8 && V * NQ == NT && Nh % BOX == 0, "one item per thread, FP32, whole boxes");
+  static_assert(S % 2 == 0 && R % 2 == 0, "paired first pass needs an even stride and radix");
+  const C* stg = sm;  // [plane][k < N/2][v]
+  if (tid == 0) {
+    mbar_expect_tx(bar, 2u * Nh * V * (unsigned)sizeof(C));
+#pragma unroll 1
+    for (int bx = 0; bx < Nh / BOX; ++bx) {
+      tma_load_3d(&maps.w0, sm + (size_t)bx * BOX * V, bar, 2 * z0, bx * BOX, (int)blockIdx.y);
+      tma_load_3d(&maps.w1, sm + (size_t)(Nh + bx * BOX) * V, bar, 2 * z0, bx * BOX, (int)blockIdx.y);
+    }
+  }
+  if (!mbar_wait(bar, 0, 1 << 22)) {
+    // the copies did not complete in time: report it and wait (bounded) for them
+    // before the shared memory is used or released
+    if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
+    mbar_wait(bar, 0, 1 << 22);
+  }
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  const int v = tid % V;
+  const int q = tid / V;
+  const bool self = q == 0;
+  const int i2 = self ? S / 2 : S - q;
+  C x[R], y[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) x[j] = y[j] = C{T(0), T(0)};
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    if (j * S >= Nh) continue;  // folded at compile time
+    const int k1 = q + j * S;
+    if (j * S + S - 1 < Nh || k1 < Nh) {
+      const C u = stg[(size_t)k1 * V + v], qv = stg[(size_t)(Nh + k1) * V + v];
+      const C m = C{u.x + qv.y, qv.x - u.y};
+      if (self) {
+        if (j == 0) {
+          x[0] = C{u.x, qv.x};
+        } else {
+          x[j] = C{u.x - qv.y, u.y + qv.x};
+          x[(R - j) % R] = m;
+        }
+      } else {
+        x[j] = C{u.x - qv.y, u.y + qv.x};
+        y[R - 1 - j] = m;
+      }
+    }
+    const int k2 = i2 + j * S;
+    if (j * S + S - 1 < Nh || k2 < Nh) {
+      const C u = stg[(size_t)k2 * V + v], qv = stg[(size_t)(Nh + k2) * V + v];
+      const C m = C{u.x + qv.y, qv.x - u.y};
+      y[j] = C{u.x - qv.y, u.y + qv.x};
+      if (self) y[R - 1 - j] = m;
+      else x[R - 1 - j] = m;
+    }
+  }
+  __syncthreads();  // every staged row is in registers: the tile is free
+  Dft<R, +1, C>::run(x);
+  pass_tw<PL, 0, +1>(x, tw, q);
+  {
+    C* p = sm + PL::phys(q) * V + v;
+#pragma unroll
+    for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
+  }
+  Dft<R, +1, C>::run(y);
+  pass_tw<PL, 0, +1>(y, tw, i2);
+  {
+    C* p = sm + PL::phys(i2) * V + v;
+#pragma unroll
+    for (int k = 0; k < R; ++k) p[k * SP * V] = y[k];
+  }
+  __syncthreads();
+}
+
 // Last forward DIT pass of the row kernel fused with the Hermitian unpack.
 // Butterfly i produces P[i + j S]; the conjugate partner P[M - i - j S] sits in
 // butterfly S - i at index R-1-j (for i = 0 in butterfly 0 at (R-j) mod R, for
@@ -379,16 +512,6 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
   }
 }
 
-// Bulk tensor stores (TMA) from shared memory.
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* smem, int x, int y, int z) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map), "r"(s),
-               "r"(x), "r"(y), "r"(z)
-               : "memory");
-}
-__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void tma_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 
 // The paired last pass with the stores handed to the TMA unit: each thread
 // (one item, V S / 2 == NT) keeps its A, B rows in registers, the block
@@ -481,6 +604,7 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
 // first, so that the block that will run it finds its rows there.
 // PF bit 1: the first pass reads every U-state row once (row_first_pass_paired).
 // PF bit 2 (value 4): the last pass stores through the TMA unit (row_last_pass_tma).
+// PF bit 3 (value 8): the first pass loads through the TMA unit (row_first_pass_tma).
 template <typename T, class PL, int V, int NT, int PF>
 __global__ void __launch_bounds__(NT) k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = cplx<T>;
@@ -501,7 +625,12 @@ __global__ void __launch_bounds__(NT) k_row(StepArgs a0, const __grid_constant__
       for (int r = tid; r < 2 * Nh; r += NT) l2_prefetch_line((r < Nh ? w0 : w1) + (size_t)(r < Nh ? r : r - Nh) * M);
     }
   }
-  if constexpr ((PF & 2) != 0) {
+  if constexpr ((PF & 8) != 0) {
+    __shared__ __align__(8) unsigned long long tma_bar;
+    if (tid == 0) mbar_init(&tma_bar, 1);
+    __syncthreads();
+    row_first_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, &tma_bar);
+  } else if constexpr ((PF & 2) != 0) {
     row_first_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
   } else {
     row_first_pass<T, PL, V, NT>(a, sm, z0, tid);

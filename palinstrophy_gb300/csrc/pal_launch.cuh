@@ -111,13 +111,13 @@ struct RowOf {
     b.ahead = ahead;
     static const TmaMaps none{};
     k_row<T, PL, V, NT, PF><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
-        b, ((PF & 4) != 0 && a.tmaps) ? *a.tmaps : none);
+        b, ((PF & 12) != 0 && a.tmaps) ? *a.tmaps : none);
   }
   static void phys(const StepArgs& a, cudaStream_t s) {
     k_phys<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
   }
   static constexpr RowKernels make(const char* name) {
-    return RowKernels{name, V, NT, (PF & 4) != 0, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
+    return RowKernels{name, V, NT, (PF & 12) != 0, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
   }
 };
 

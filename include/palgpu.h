@@ -165,6 +165,9 @@ int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, d
  * control; no counterpart in the reference. */
 int pal_get_variant(pal_handle* h, int* row, int* col, int* n_rows, int* n_cols, char* desc, size_t desc_len);
 int pal_set_variant(pal_handle* h, int row, int col);
+/* Resident blocks per SM of the selected row and column kernels, from the CUDA
+ * occupancy calculator (diagnostic; no counterpart in the reference). */
+int pal_get_occupancy(pal_handle* h, int* row_blocks_per_sm, int* col_blocks_per_sm);
 /* The handle's CUDA stream (cudaStream_t), for event timing or interop. */
 int pal_get_stream(pal_handle* h, void** stream);
 int pal_last_error(pal_handle* h, char* buf, size_t n);

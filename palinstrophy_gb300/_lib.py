@@ -78,6 +78,7 @@ _SIGS = {
     "pal_get_variant": (_I, [_H, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                              ctypes.c_char_p, ctypes.c_size_t]),
     "pal_set_variant": (_I, [_H, _I, _I]),
+    "pal_get_occupancy": (_I, [_H, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "pal_profile_kernels": (_I, [_H, _I, _I, _DP, _DP, ctypes.POINTER(_I)]),
     "pal_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
     "pal_ensemble_create": (_I, [_I, ctypes.POINTER(_I), _I, _D, _D, ctypes.POINTER(_H)]),

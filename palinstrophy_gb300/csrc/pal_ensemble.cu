@@ -151,6 +151,7 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
         a.beta = kRkBeta[s];
       }
       a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
+      if (method != PAL_CNAB2) pal::rk3_stage_flags(a, s, kRkBeta);
       g.ck->col_perm(a, e->stream);
     }
   }

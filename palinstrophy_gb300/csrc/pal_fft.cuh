@@ -299,6 +299,23 @@ struct Rec : PL {
   static constexpr int TW_TOTAL = tw_off(PL::NP);
 };
 
+// Compact tables for pass 0 (large stride) and full tables for the later
+// passes, stored transposed as [k/2][i] pairs (W^(2k' i), W^((2k'+1) i)) so the
+// lanes of a warp, which hold consecutive butterflies i, read consecutive
+// 16-byte entries.  The later passes have small strides (tables of a few KB
+// that stay in L1), and each of their butterflies then spends R/2 loads
+// instead of the products that form the powers.  FP32 only.
+template <class PL>
+struct RecT : PL {
+  static constexpr int TW_MODE = 2;
+  static constexpr int tw_off(int p) {
+    int o = 0;
+    for (int q = 0; q < p; ++q) o += q == 0 ? 2 * PL::stride(q) : PL::stride(q) * PL::R[q];
+    return o;
+  }
+  static constexpr int TW_TOTAL = tw_off(PL::NP);
+};
+
 // x * W^(SIGN) where w = exp(-2 pi i e / L) is a forward-table entry.
 template <int SIGN, typename C>
 __device__ __forceinline__ C twmul(C x, C w) {
@@ -367,6 +384,16 @@ template <class PL, int P, int SIGN, int R, typename C>
 __device__ __forceinline__ void pass_tw(C (&x)[R], const C* __restrict__ tw, int i) {
   if constexpr (PL::TW_MODE == 0) {
     apply_tw<R, SIGN>(x, tw + PL::tw_off(P) + i * R);
+  } else if constexpr (PL::TW_MODE == 2 && P >= 1) {
+    static_assert(sizeof(C) == 8 && R % 2 == 0, "transposed pair tables are FP32, even radix");
+    constexpr int S = PL::stride(P);
+    const float4* __restrict__ t = reinterpret_cast<const float4*>(tw + PL::tw_off(P)) + i;
+#pragma unroll
+    for (int k2 = 0; k2 < R / 2; ++k2) {
+      const float4 v = __ldg(t + k2 * S);
+      if (k2 > 0) x[2 * k2] = twmul<SIGN>(x[2 * k2], C{v.x, v.y});
+      x[2 * k2 + 1] = twmul<SIGN>(x[2 * k2 + 1], C{v.z, v.w});
+    }
   } else {
     const C* t = tw + PL::tw_off(P) + 2 * i;
     C w1, w4;
@@ -440,11 +467,20 @@ __device__ __forceinline__ double tw_angle(int e) {
     constexpr int R = PL::R[Q];
     constexpr int S = PL::stride(Q);
     constexpr int step = PL::M / PL::span(Q);
-    constexpr int W = PL::TW_MODE == 0 ? R : 2;  // entries per butterfly
+    constexpr bool FULL_T = PL::TW_MODE == 2 && Q >= 1;      // transposed [k/2][i] pairs
+    constexpr int W = (PL::TW_MODE == 0 || FULL_T) ? R : 2;  // entries per butterfly
     if (e < off + S * W) {
-      const int i = (e - off) / W;
-      const int c = (e - off) - i * W;
-      const int k = PL::TW_MODE == 0 ? c : (c == 0 ? 1 : 4);
+      int i, k;
+      if constexpr (FULL_T) {
+        const int r = e - off;
+        const int k2 = r / (2 * S);
+        i = (r - k2 * 2 * S) / 2;
+        k = 2 * k2 + (r & 1);
+      } else {
+        i = (e - off) / W;
+        const int c = (e - off) - i * W;
+        k = PL::TW_MODE == 0 ? c : (c == 0 ? 1 : 4);
+      }
       return 2.0 * (double)((long long)step * i * k) / (double)PL::M;
     }
     return tw_angle<PL, Q + 1>(e);

@@ -13,11 +13,13 @@ const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"
                             RowOf<float, Rec<P12288>, 2, 512, 3>::make("16.32.24r V2x512 paired l2pf"),
                             RowOf<float, Rec<P12288>, 2, 768, 7>::make("16.32.24r V2x768 paired l2pf tma"),
                             RowOf<float, Rec<P12288>, 2, 768, 15>::make("16.32.24r V2x768 tma-in tma-out l2pf"),
-                            RowOf<float, Rec<P12288>, 2, 768, 11>::make("16.32.24r V2x768 tma-in l2pf")};
+                            RowOf<float, Rec<P12288>, 2, 768, 11>::make("16.32.24r V2x768 tma-in l2pf"),
+                            RowOf<float, RecT<P12288>, 2, 768, 15>::make("16.32.24t V2x768 tma-in tma-out l2pf")};
 const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
                             ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),
-                            ColOf<float, Rec<P12288>, 512, 3>::make("16.32.24r x512 hoist pipe0")};
+                            ColOf<float, Rec<P12288>, 512, 3>::make("16.32.24r x512 hoist pipe0"),
+                            ColOf<float, RecT<P12288>, 512, 3>::make("16.32.24t x512 hoist pipe0")};
 
 PAL_KERNEL_SET(float, 0, 8192, r8192, c8192)
 }  // namespace

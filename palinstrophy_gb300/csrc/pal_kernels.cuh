@@ -29,6 +29,10 @@ enum : int {
   F_ADVANCE = 4,    // k_col: t += dt, it += 1 in the epilogue
   F_CNM1 = 8,       // k_col: cnm1 = cn in the epilogue (CNAB2)
   F_PHYS = 16,      // k_phys: store the physical u, v planes
+  // k_col, LS-IMEX-RK3 stages on butterfly-major om / fnm1 (om_p, fm_p):
+  F_NO_FM_IN = 32,  // the update does not read fnm1 (its weight c3 is 0: first stage)
+  F_Q_IN = 64,      // om holds q = (1 - K2 h1) om + c3 fnm1 of this stage; fnm1 is not read
+  F_Q_OUT = 128,    // write the next stage's q (weights from beta_next) into om, not om and fn
 };
 
 // Device-resident scalars, FP64 in both precisions.
@@ -58,6 +62,7 @@ struct StepArgs {
   double h1, h2;    // implicit factors: rhs = 1 - K2*h1, den = 1 + K2*h2 (if from_dt == 0)
   double c2, c3;    // explicit weights of fn and fnm1
   double alpha, beta;
+  double beta_next;  // RK3: beta of the next stage (F_Q_OUT)
   int scheme;       // 0 = CNAB2 (coefficients from device dt/cnm1), 1 = RK3 stage
   // Batched ensembles: blockIdx.y selects the member; every per-member array
   // advances by its stride (in elements) and sc by one DevScalars per member.
@@ -605,8 +610,18 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
 // PF bit 1: the first pass reads every U-state row once (row_first_pass_paired).
 // PF bit 2 (value 4): the last pass stores through the TMA unit (row_last_pass_tma).
 // PF bit 3 (value 8): the first pass loads through the TMA unit (row_first_pass_tma).
+// PF bit 4 (value 16): registers are capped so that as many blocks share an SM
+// as its shared memory holds tiles (row_tiles_per_sm); without it the
+// launch bound names no block count and the compiler chooses.
+template <typename T, class PL, int V>
+constexpr int row_tiles_per_sm() {
+  // 228 KB of shared memory per SM, 1 KB of it reserved per block, plus the
+  // block's static shared memory (mbarrier, reduction scratch)
+  return int(size_t(228 * 1024) / (size_t(PL::PADM) * V * sizeof(cplx<T>) + 1024 + 256));
+}
 template <typename T, class PL, int V, int NT, int PF>
-__global__ void __launch_bounds__(NT) k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
+__global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() : 0)
+    k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
   extern __shared__ __align__(128) unsigned char smraw[];
@@ -738,6 +753,7 @@ __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
 template <typename T>
 struct ModeCoef {
   T h1, h2, c2, c3, divxz;
+  T h1n, c3n;  // the next RK3 stage's h1 and c3 (F_Q_OUT)
 };
 
 // 16-byte asynchronous global -> shared copies (Ampere+ cp.async).
@@ -767,6 +783,8 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
     c2 = a.alpha * dt;
     c3 = a.beta * dt;
   }
+  cf.h1n = a.scheme == 0 ? T(0) : T((a.beta_next * dt) * visc);
+  cf.c3n = a.scheme == 0 ? T(0) : T(a.beta_next * dt);
   cf.h1 = T(h1);
   cf.h2 = T(h2);
   cf.c2 = T(c2);
@@ -787,10 +805,21 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
 // lane requests all its om / fm values before the butterfly's shared-memory
 // loads and DFT, so their latency overlaps that work (the update loop stores
 // to om / fm, so the compiler cannot move later loads above earlier stores).
+//
+// Within an LS-IMEX-RK3 step the stage update
+//   om' = ((1 - K2 h1) om + c2 fn + c3 fnm1) / (1 + K2 h2)
+// uses om and fnm1 only through q = (1 - K2 h1) om + c3 fnm1, and the next
+// stage's weights are known when a stage ends.  With F_Q_OUT a stage stores
+// that q for the next stage in place of om (and no fn); with F_Q_IN the stage
+// reads q and no fnm1; F_NO_FM_IN skips the fnm1 read of the first stage,
+// whose c3 is 0.  The last stage stores om and fn as the reference state.
 template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false>
 __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
                                            cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
-                                           const ModeCoef<T>& cf, int kx, int tid) {
+                                           const ModeCoef<T>& cf, int kx, int tid, int flags) {
+  const bool q_in = (flags & F_Q_IN) != 0;
+  const bool fm_in = (flags & (F_Q_IN | F_NO_FM_IN)) == 0;
+  const bool q_out = (flags & F_Q_OUT) != 0;
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int V = 2;
@@ -820,7 +849,7 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
         const int zi = PERM ? (j + v) * FSTEP + b : z;
         if (act && (BAND_CT || f < Nh || f >= N)) {
           h_o[jj] = om[zi];
-          h_f[jj] = fm[zi];
+          if (fm_in) h_f[jj] = fm[zi];
         }
       }
     }
@@ -849,7 +878,8 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       const int zi = PERM ? (j + v) * FSTEP + b : z;
       if (inband) {
         const C o = SMEM_OM ? s_om[z] : (HOIST ? h_o[j / 2] : om[zi]);
-        const C fo = SMEM_OM ? s_fm[z] : (HOIST ? h_f[j / 2] : fm[zi]);
+        C fo = {T(0), T(0)};
+        if (fm_in) fo = SMEM_OM ? s_fm[z] : (HOIST ? h_f[j / 2] : fm[zi]);
         const T gz = T(z < Nh ? z : z - N);
         const T K2 = ax * ax + gz * gz;
         const T GA = gz * ax;
@@ -859,13 +889,23 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
           fn.x = (Az.x * GA + Bz.x * G2mA2) * cf.divxz;
           fn.y = (Az.y * GA + Bz.y * G2mA2) * cf.divxz;
         }
-        const T c1 = T(1) - K2 * cf.h1;
         const T rden = T(1) / (T(1) + K2 * cf.h2);
         C on;
-        on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
-        on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
-        om[zi] = on;
-        fm[zi] = fn;
+        if (q_in) {
+          on.x = (o.x + cf.c2 * fn.x) * rden;
+          on.y = (o.y + cf.c2 * fn.y) * rden;
+        } else {
+          const T c1 = T(1) - K2 * cf.h1;
+          on.x = (c1 * o.x + cf.c2 * fn.x + cf.c3 * fo.x) * rden;
+          on.y = (c1 * o.y + cf.c2 * fn.y + cf.c3 * fo.y) * rden;
+        }
+        if (q_out) {
+          const T c1n = T(1) - K2 * cf.h1n;
+          om[zi] = C{c1n * on.x + cf.c3n * fn.x, c1n * on.y + cf.c3n * fn.y};
+        } else {
+          om[zi] = on;
+          fm[zi] = fn;
+        }
         if (kx >= 1) {
           const T ik = T(1) / K2;
           const C t = {on.x * ik, on.y * ik};
@@ -1025,7 +1065,8 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     cp_async_wait_all();
     __syncthreads();
   }
-  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3>(sm, s_om, s_fm, om, fm, cf, kx, tid);
+  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3>(sm, s_om, s_fm, om, fm, cf, kx, tid,
+                                                                         a.flags);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
   col_finish<NT>(a, tid);

@@ -22,6 +22,7 @@ struct RowKernels {
   void (*row)(const StepArgs&, cudaStream_t);
   void (*phys)(const StepArgs&, cudaStream_t);
   void (*twiddles)(void* tw, cudaStream_t);
+  int (*blocks_per_sm)();  // resident k_row blocks per SM (occupancy calculator)
 };
 
 struct ColKernels {
@@ -38,6 +39,7 @@ struct ColKernels {
   void (*col_perm)(const StepArgs&, cudaStream_t);
   void (*to_perm)(const StepArgs&, cudaStream_t);
   void (*from_perm)(const StepArgs&, cudaStream_t);
+  int (*blocks_per_sm)();  // resident k_col blocks per SM (occupancy calculator)
 };
 
 // Adjoint of one LS-IMEX-RK3 stage (pal_adjoint.cuh), on fixed plans.
@@ -93,6 +95,15 @@ inline int wave_blocks(K kernel, int nt, size_t smem) {
   return sms * per_sm;
 }
 
+// Column-pass flags of LS-IMEX-RK3 stage s (0..2) on butterfly-major om /
+// fnm1: the first stage reads no fnm1, the first two hand the next stage its
+// combined q in om (k_col F_Q_OUT / F_Q_IN), the last stores om and fn.
+// `beta` is the stage table of beta coefficients.
+inline void rk3_stage_flags(StepArgs& a, int s, const double* beta) {
+  a.flags |= (s == 0 ? F_NO_FM_IN : F_Q_IN) | (s < 2 ? F_Q_OUT : 0);
+  a.beta_next = s < 2 ? beta[s + 1] : 0.0;
+}
+
 template <typename T, class PL, int V, int NT, int PF = 0>
 struct RowOf {
   static constexpr size_t smem = size_t(PL::PADM) * V * sizeof(cplx<T>);
@@ -102,6 +113,11 @@ struct RowOf {
   static cudaError_t configure() {
     cudaError_t e =
         cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    // ask for the largest shared-memory carveout, so that every tile that fits
+    // twice per SM is resident twice whatever ran before
+    e = cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     if (PF & 1) ahead = wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -116,8 +132,13 @@ struct RowOf {
   static void phys(const StepArgs& a, cudaStream_t s) {
     k_phys<T, PL, V, NT><<<dim3(PL::M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(a);
   }
+  static int blocks_per_sm() {
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_row<T, PL, V, NT, PF>, NT, smem) == cudaSuccess ? n : -1;
+  }
   static constexpr RowKernels make(const char* name) {
-    return RowKernels{name, V, NT, (PF & 12) != 0, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>};
+    return RowKernels{name, V,   NT, (PF & 12) != 0, smem, PL::TW_TOTAL, configure, row, phys, launch_twiddles<T, PL>,
+                      blocks_per_sm};
   }
 };
 
@@ -134,6 +155,9 @@ struct ColOf {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_inv);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_om_perm<T, PL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_perm);
     if (e != cudaSuccess) return e;
@@ -157,9 +181,16 @@ struct ColOf {
   static void col_inv(const StepArgs& a, cudaStream_t s) {
     k_col_inv<T, PL, NT><<<dim3(a.N / 2, a.members > 1 ? a.members : 1), NT, smem_inv, s>>>(a);
   }
+  static int blocks_per_sm() {
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true>, NT, smem_inv) ==
+                   cudaSuccess
+               ? n
+               : -1;
+  }
   static constexpr ColKernels make(const char* name) {
     return ColKernels{name,    NT,     smem,     PL::TW_TOTAL,          configure, col,
-                      col_inv, launch_twiddles<T, PL>, col_perm, to_perm, from_perm};
+                      col_inv, launch_twiddles<T, PL>, col_perm, to_perm, from_perm, blocks_per_sm};
   }
 };
 

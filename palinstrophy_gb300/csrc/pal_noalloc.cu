@@ -134,6 +134,7 @@ extern "C" int pal_step_noalloc(int N, int method, int nsteps, double dt, double
         a.scheme = 1;
         a.alpha = alpha[st];
         a.beta = beta[st];
+        pal::rk3_stage_flags(a, st, beta);  // the same stage arithmetic as pal_step
         a.tw = tw_col;
         ck.col(a, s);
       }

@@ -176,8 +176,10 @@ class Field:
         buf = L.ctypes.create_string_buffer(256)
         self._ck(self.lib.pal_get_variant(self.h, L.ctypes.byref(r), L.ctypes.byref(c), L.ctypes.byref(nr),
                                           L.ctypes.byref(nc), buf, len(buf)))
+        rb, cb = L._I(), L._I()
+        self._ck(self.lib.pal_get_occupancy(self.h, L.ctypes.byref(rb), L.ctypes.byref(cb)))
         return {"row": r.value, "col": c.value, "n_rows": nr.value, "n_cols": nc.value,
-                "desc": buf.value.decode()}
+                "desc": buf.value.decode(), "row_blocks_per_sm": rb.value, "col_blocks_per_sm": cb.value}
 
     def set_variant(self, row: int, col: int):
         self._ck(self.lib.pal_set_variant(self.h, int(row), int(col)))

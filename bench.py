@@ -424,7 +424,7 @@ def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100
     big = {"N": N, "dtype": "f32", "steps": steps_8192, "steps_per_s": 1000.0 / ms, "ms_per_step": ms,
            "kernels": variant,
            "k_row": {"ms": ms_row, "algorithmic_GBps": 6.0 * n2 * s_bytes / (ms_row / 1000.0) / 1e9},
-           "k_col": {"ms": ms_col, "algorithmic_GBps": 10.0 * n2 * s_bytes / (ms_col / 1000.0) / 1e9}}
+           "k_col": {"ms": ms_col, "algorithmic_GBps": (25.0 / 3.0) * n2 * s_bytes / (ms_col / 1000.0) / 1e9}}
     hist = {}
     for prec in ("fp32", "fp64"):
         G = _field(prec, om2, uc, visc)
@@ -561,7 +561,10 @@ def run_gb300(args):
     s_bytes = 4
     n2 = float(N_GRID) * N_GRID
     bytes_row = 6.0 * n2 * s_bytes   # read + write 2 planes of (N/2 x 3N/2) complex
-    bytes_col = 10.0 * n2 * s_bytes  # the same + read/write om2 and fnm1 (N x N/2 complex)
+    # the same planes + the om / fnm1 traffic of an LS-IMEX-RK3 step's three
+    # column passes, in arrays of N x N/2 complex (1.0 n2 s_bytes each way):
+    # om in + q out, q in + q out, q in + om and fnm1 out -> (8 + 8 + 9) / 3
+    bytes_col = (25.0 / 3.0) * n2 * s_bytes
     dominant = "k_col" if ms_col >= ms_row else "k_row"
     dom_ms = max(ms_col, ms_row)
     dom_bytes = bytes_col if dominant == "k_col" else bytes_row

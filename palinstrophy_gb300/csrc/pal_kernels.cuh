@@ -813,13 +813,15 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
 // that q for the next stage in place of om (and no fn); with F_Q_IN the stage
 // reads q and no fnm1; F_NO_FM_IN skips the fnm1 read of the first stage,
 // whose c3 is 0.  The last stage stores om and fn as the reference state.
-template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false>
+// QM: the F_Q_* / F_NO_FM_IN flags are honoured (a separate instantiation, so
+// that the plain update keeps its register budget).
+template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false, bool QM = false>
 __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
                                            cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
                                            const ModeCoef<T>& cf, int kx, int tid, int flags) {
-  const bool q_in = (flags & F_Q_IN) != 0;
-  const bool fm_in = (flags & (F_Q_IN | F_NO_FM_IN)) == 0;
-  const bool q_out = (flags & F_Q_OUT) != 0;
+  const bool q_in = QM && (flags & F_Q_IN) != 0;
+  const bool fm_in = !QM || (flags & (F_Q_IN | F_NO_FM_IN)) == 0;
+  const bool q_out = QM && (flags & F_Q_OUT) != 0;
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int V = 2;
@@ -979,7 +981,8 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
 // hoists each lane's om / fnm1 loads above its DFT (col_middle HOIST), PREF == 3
 // also overlaps the pass-0 loads of a thread's next butterfly.  With
 // PERM the kernel works on om_p / fm_p (butterfly-major columns of M elements).
-template <typename T, class PL, int NT, int PREF, bool PERM>
+// QM: the RK3 stage flags F_Q_IN / F_Q_OUT / F_NO_FM_IN are honoured (col_middle).
+template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C));
@@ -1065,8 +1068,8 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
     cp_async_wait_all();
     __syncthreads();
   }
-  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3>(sm, s_om, s_fm, om, fm, cf, kx, tid,
-                                                                         a.flags);
+  col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3, QM>(sm, s_om, s_fm, om, fm, cf, kx,
+                                                                             tid, a.flags);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
   col_finish<NT>(a, tid);

@@ -74,6 +74,7 @@ struct KernelSet {
 
 constexpr int kSpectralThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;
+constexpr size_t kLargeTile = 64 * 1024;  // tiles from this size on ask for the max shared carveout
 
 // TMA descriptors of the planes w0 / w1 (members x N/2 rows x M complex FP32)
 // for a row candidate with tile height V; false if the driver call is missing
@@ -114,11 +115,14 @@ struct RowOf {
     cudaError_t e =
         cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    // ask for the largest shared-memory carveout, so that every tile that fits
-    // twice per SM is resident twice whatever ran before
-    e = cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
+    // tiles of 64 KB and more ask for the largest shared-memory carveout, so that
+    // two of them are resident per SM whatever ran before; smaller tiles leave
+    // the split to the driver (their L1 holds the twiddle tables and planes)
+    if (smem >= kLargeTile) {
+      e = cudaFuncSetAttribute(k_row<T, PL, V, NT, PF>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+    }
     if (PF & 1) ahead = wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
@@ -156,9 +160,17 @@ struct ColOf {
     e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_inv);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
+    e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_inv);
     if (e != cudaSuccess) return e;
+    if (smem_inv >= kLargeTile) {
+      e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true, false>,
+                               cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+    }
     e = cudaFuncSetAttribute(k_om_perm<T, PL, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_perm);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_om_perm<T, PL, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_perm);
@@ -167,8 +179,13 @@ struct ColOf {
   }
   static dim3 grid(const StepArgs& a) { return dim3(a.N / 2, a.members > 1 ? a.members : 1); }
   static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF, false><<<grid(a), NT, smem, s>>>(a); }
+  // RK3 stages carrying the combined term run the flag-aware instantiation;
+  // every other butterfly-major column pass runs the plain update
   static void col_perm(const StepArgs& a, cudaStream_t s) {
-    k_col<T, PL, NT, PERM_PREF, true><<<grid(a), NT, smem_inv, s>>>(a);
+    if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
+      k_col<T, PL, NT, PERM_PREF, true, true><<<grid(a), NT, smem_inv, s>>>(a);
+    else
+      k_col<T, PL, NT, PERM_PREF, true, false><<<grid(a), NT, smem_inv, s>>>(a);
   }
   static constexpr size_t smem_perm = size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>);  // one om + fnm1 column
   static_assert(smem_perm <= kSmemLimit, "om / fnm1 column does not fit in shared memory");
@@ -183,7 +200,7 @@ struct ColOf {
   }
   static int blocks_per_sm() {
     int n = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true>, NT, smem_inv) ==
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true, false>, NT, smem_inv) ==
                    cudaSuccess
                ? n
                : -1;

@@ -23,7 +23,7 @@ def test_traffic_and_limiter_come_from_the_profiles(bench):
     t_row = bench._traffic("k_row", "fp32")
     t_col = bench._traffic("k_col", "fp32")
     assert t_row is not None and 3.0e8 < t_row < 5.0e8  # ~0.35 GB per N=4096 launch
-    assert t_col is not None and 5.0e8 < t_col < 8.0e8
+    assert t_col is not None and 4.0e8 < t_col < 8.0e8  # 0.47-0.61 GB by RK3 stage
     lim = bench._limiter("k_row", "fp32")
     assert lim and "issue" in lim and "profiles/k_row_fp32_N4096.md" in lim
     assert bench._traffic("k_nonexistent", "fp32") is None

@@ -79,7 +79,7 @@ bool encode_row_maps(TmaMaps* out, void* w0, void* w1, int N, int V, int members
   const int M = 3 * N / 2, Nh = N / 2;
   const cuuint64_t dims[3] = {(cuuint64_t)2 * M, (cuuint64_t)Nh, (cuuint64_t)members};
   const cuuint64_t strides[2] = {(cuuint64_t)M * 8, (cuuint64_t)Nh * M * 8};  // bytes, dims 1 and 2
-  const cuuint32_t box[3] = {(cuuint32_t)(2 * V), 256, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * V), (cuuint32_t)tma_box_rows(Nh), 1};
   const cuuint32_t elem[3] = {1, 1, 1};
   void* base[2] = {w0, w1};
   CUtensorMap* maps[2] = {&out->w0, &out->w1};

@@ -76,9 +76,18 @@ struct StepArgs {
   const struct TmaMaps* tmaps;  // host: descriptors of w0 / w1 for the row pass's bulk stores
 };
 
+// Rows per TMA box of the row tiles: the largest power of two up to 256 that
+// divides the N/2 stored rows (box dimensions are at most 256).
+__host__ __device__ constexpr int tma_box_rows(int nh) {
+  int b = 256;
+  while (b > 1 && nh % b != 0) b /= 2;
+  return b;
+}
+
 // TMA descriptors of the two work planes, each a 3D view (2M floats, N/2 rows,
-// members) with a (2V floats, 256 rows, 1) box: one box is 256 rows of one row
-// tile.  Passed to the row kernel as a __grid_constant__ parameter.
+// members) with a (2V floats, tma_box_rows(N/2) rows, 1) box: one box is that
+// many rows of one row tile.  Passed to the row kernel as a __grid_constant__
+// parameter.
 struct TmaMaps {  // aligned as CUtensorMap
   CUtensorMap w0, w1;
 };
@@ -383,9 +392,11 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
   constexpr int SP = PL::pstride(0);
   constexpr int Nh = M / 3;
   constexpr int NQ = S / 2;
-  constexpr int BOX = 256;
-  static_assert(sizeof(C) == 8 && V * NQ == NT && Nh % BOX == 0, "one item per thread, FP32, whole boxes");
+  constexpr int BOX = tma_box_rows(Nh);
+  // one item per thread; threads beyond the V*NQ items only join the barriers
+  static_assert(sizeof(C) == 8 && V * NQ <= NT && BOX >= 32, "one item per thread, FP32, boxes of 32+ rows");
   static_assert(S % 2 == 0 && R % 2 == 0, "paired first pass needs an even stride and radix");
+  const bool live = V * NQ == NT || tid < V * NQ;
   const C* stg = sm;  // [plane][k < N/2][v]
   if (tid == 0) {
     mbar_expect_tx(bar, 2u * Nh * V * (unsigned)sizeof(C));
@@ -411,7 +422,7 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
   for (int j = 0; j < R; ++j) x[j] = y[j] = C{T(0), T(0)};
 #pragma unroll
   for (int j = 0; j < R; ++j) {
-    if (j * S >= Nh) continue;  // folded at compile time
+    if (j * S >= Nh || !live) continue;  // the first test folds at compile time
     const int k1 = q + j * S;
     if (j * S + S - 1 < Nh || k1 < Nh) {
       const C u = stg[(size_t)k1 * V + v], qv = stg[(size_t)(Nh + k1) * V + v];
@@ -438,19 +449,21 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
     }
   }
   __syncthreads();  // every staged row is in registers: the tile is free
-  Dft<R, +1, C>::run(x);
-  pass_tw<PL, 0, +1>(x, tw, q);
-  {
-    C* p = sm + PL::phys(q) * V + v;
+  if (live) {
+    Dft<R, +1, C>::run(x);
+    pass_tw<PL, 0, +1>(x, tw, q);
+    {
+      C* p = sm + PL::phys(q) * V + v;
 #pragma unroll
-    for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
-  }
-  Dft<R, +1, C>::run(y);
-  pass_tw<PL, 0, +1>(y, tw, i2);
-  {
-    C* p = sm + PL::phys(i2) * V + v;
+      for (int k = 0; k < R; ++k) p[k * SP * V] = x[k];
+    }
+    Dft<R, +1, C>::run(y);
+    pass_tw<PL, 0, +1>(y, tw, i2);
+    {
+      C* p = sm + PL::phys(i2) * V + v;
 #pragma unroll
-    for (int k = 0; k < R; ++k) p[k * SP * V] = y[k];
+      for (int k = 0; k < R; ++k) p[k * SP * V] = y[k];
+    }
   }
   __syncthreads();
 }
@@ -534,12 +547,14 @@ __device__ __forceinline__ void row_last_pass_tma(const StepArgs& a, cplx<T>* sm
   constexpr int Nh = M / 3;
   constexpr int NQ = S / 2;
   constexpr int JN = (Nh + S - 1) / S;  // j with j S < N/2
-  constexpr int BOX = 256;
-  static_assert(sizeof(C) == 8 && V * NQ == NT && Nh % BOX == 0, "one item per thread, FP32, whole boxes");
+  constexpr int BOX = tma_box_rows(Nh);
+  // one item per thread; threads beyond the V*NQ items only join the barriers
+  static_assert(sizeof(C) == 8 && V * NQ <= NT && BOX >= 32, "one item per thread, FP32, boxes of 32+ rows");
   static_assert(size_t(2) * Nh * V <= size_t(PL::PADM) * V, "staging fits in the tile");
+  const bool live = V * NQ == NT || tid < V * NQ;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   const int v = tid % V;
-  const int q = tid / V;
+  const int q = live ? tid / V : 0;
   const bool self = q == 0;
   const int i2 = self ? S / 2 : S - q;
   C y1[R], y2[R];
@@ -571,6 +586,7 @@ __device__ __forceinline__ void row_last_pass_tma(const StepArgs& a, cplx<T>* sm
   C* stg = sm;      // [plane][k < N/2][v]
 #pragma unroll
   for (int j = 0; j < JN; ++j) {
+    if (!live) break;
     const int k1 = q + j * S, k2 = i2 + j * S;
     if (k1 < Nh) {
       stg[(size_t)k1 * V + v] = A1[j];

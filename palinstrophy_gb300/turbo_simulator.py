@@ -621,6 +621,11 @@ class Ensemble:
         self._ck(self.lib.pal_ensemble_get_member(self.h, int(m), L.PAL_FIELD_OM2, L.ptr(a)))
         return a
 
+    def fnm1(self, m):
+        a = np.empty((self.Ns[m], self.Ns[m] // 2), self.cdt)
+        self._ck(self.lib.pal_ensemble_get_member(self.h, int(m), L.PAL_FIELD_FNM1, L.ptr(a)))
+        return a
+
     def scalars(self, m):
         v = [L._D() for _ in range(4)]
         it = L.ctypes.c_longlong()

@@ -156,3 +156,32 @@ def test_batched_autotune(ts):
         assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
         F.close()
     E.close()
+
+
+def test_members_with_bulk_tensor_row_loads(ts):
+    """Members of 1024 and 2048 (sizes whose tuned row kernels load and store
+    their tiles with TMA bulk tensor copies through per-group descriptors with
+    a member dimension) step exactly like single fields."""
+    Ns = [1024, 2048, 1024]
+    seeds = [2, 4, 6]
+    E = ts.Ensemble(Ns, "fp32", 1e4, 0.5)
+    for m, (n, sd) in enumerate(zip(Ns, seeds)):
+        om2, uc, st = _member_init(n, sd)
+        E.set_member(m, om2, None, uc)
+        E.set_scalar(m, "visc", st["visc"])
+    E.init_dt()
+    E.step("LS_IMEX_RK3", 6, update=3, graph=True)
+    E.synchronize()
+    for m, (n, sd) in enumerate(zip(Ns, seeds)):
+        om2, uc, st = _member_init(n, sd)
+        F = ts.Field(n, "fp32", 1e4, 0.5)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.step2a()
+        F.set_scalar("dt", 0.5 / (F.compute_cflm() * math.pi))
+        F.step("LS_IMEX_RK3", 6, update=3)
+        assert F.variant()["desc"] == E.variant(n)
+        assert np.array_equal(F.om2(), E.om2(m)), m
+        assert np.array_equal(F.fnm1(), E.fnm1(m)), m
+        F.close()
+    E.close()

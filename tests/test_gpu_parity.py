@@ -295,7 +295,7 @@ def test_dropin_run_dns(ts, capsys):
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 2e-6)])
-@pytest.mark.parametrize("N", [256, 512, 1024, 1536, 2048, 3072, 4096, 8192])
+@pytest.mark.parametrize("N", [256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096, 8192])
 def test_every_kernel_candidate_agrees(ts, prec, tol, N):
     """Each compiled row/column candidate (radix order, tile height, threads)
     gives the same field, so the autotuner's choice never changes results

@@ -626,6 +626,7 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
 // PF bit 1: the first pass reads every U-state row once (row_first_pass_paired).
 // PF bit 2 (value 4): the last pass stores through the TMA unit (row_last_pass_tma).
 // PF bit 3 (value 8): the first pass loads through the TMA unit (row_first_pass_tma).
+// PF bit 5 (value 32): with bit 0, the prefetched tile is two waves ahead.
 // PF bit 4 (value 16): registers are capped so that as many blocks share an SM
 // as its shared memory holds tiles (row_tiles_per_sm); without it the
 // launch bound names no block count and the compiler chooses.

@@ -486,3 +486,24 @@ def test_step_graph_replay_equals_direct_launches(ts, method, monkeypatch):
     assert np.array_equal(out["1"][0], out["0"][0])
     for k in ("t", "dt", "cn", "cnm1", "it"):
         assert out["1"][1][k] == out["0"][1][k], k
+
+
+def test_two_row_tiles_share_an_sm(ts):
+    """The 2-row FP32 row tiles at N=4096 (102.4 KB of shared memory each) are
+    built to run two per SM; the occupancy calculator must agree, so a register
+    budget that grows past the cap shows up here and not only as a slower step."""
+    from palinstrophy_gb300 import _lib as L
+    if not L.supported(4096, "fp32"):
+        pytest.skip("fp32 is not compiled for N=4096")
+    F = ts.Field(4096, "fp32", 1e5, 0.1)
+    v = F.variant()
+    assert v["row_blocks_per_sm"] >= 1 and v["col_blocks_per_sm"] >= 1
+    seen = 0
+    for r in range(v["n_rows"]):
+        F.set_variant(r, v["col"])
+        w = F.variant()
+        if "V2x384" in w["desc"]:
+            seen += 1
+            assert w["row_blocks_per_sm"] == 2, w["desc"]
+    assert seen >= 2
+    F.close()

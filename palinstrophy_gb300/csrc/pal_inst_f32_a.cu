@@ -25,7 +25,8 @@ const RowKernels r256[] = {RowOf<float, P384, 4, 256>::make("16.24 V4x256"),
                            RowOf<float, Rec<P384b>, 4, 256, 2>::make("24.16r V4x256 paired"),
                            RowOf<float, Rec<P384>, 4, 128, 15>::make("16.24r V4x128 tma-in tma-out l2pf"),
                            RowOf<float, Rec<P384>, 4, 256, 15>::make("16.24r V4x256 tma-in tma-out l2pf"),
-                           RowOf<float, Rec<P384b>, 4, 128, 15>::make("24.16r V4x128 tma-in tma-out l2pf")};
+                           RowOf<float, Rec<P384b>, 4, 128, 15>::make("24.16r V4x128 tma-in tma-out l2pf"),
+                           RowOf<float, Rec<P384>, 4, 128, 14>::make("16.24r V4x128 tma-in tma-out")};
 const ColKernels c256[] = {ColOf<float, P384, 128>::make("16.24 x128"), ColOf<float, P384, 64>::make("16.24 x64"),
                            ColOf<float, P384b, 128>::make("24.16 x128"),
                            ColOf<float, Rec<P384>, 128, 2>::make("16.24r x128 hoist"),

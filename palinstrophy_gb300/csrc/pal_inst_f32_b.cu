@@ -17,7 +17,8 @@ const RowKernels r2048[] = {RowOf<float, P3072, 4, 512>::make("16.8.24 V4x512"),
                             RowOf<float, P3072, 1, 256>::make("16.8.24 V1x256"),
                             RowOf<float, P3072b, 2, 256>::make("8.16.24 V2x256"),
                             RowOf<float, Rec<P3072>, 4, 384, 31>::make("16.8.24r V4x384 tma-in tma-out l2pf"),
-                            RowOf<float, Rec<P3072>, 2, 192, 31>::make("16.8.24r V2x192 tma-in tma-out l2pf")};
+                            RowOf<float, Rec<P3072>, 2, 192, 31>::make("16.8.24r V2x192 tma-in tma-out l2pf"),
+                            RowOf<float, Rec<P3072>, 4, 384, 30>::make("16.8.24r V4x384 tma-in tma-out")};
 const ColKernels c2048[] = {ColOf<float, P3072, 256>::make("16.8.24 x256"), ColOf<float, P3072, 512>::make("16.8.24 x512"),
                             ColOf<float, P3072b, 256>::make("8.16.24 x256"),
                             ColOf<float, Rec<P3072b>, 256>::make("8.16.24r x256"),
@@ -30,7 +31,8 @@ const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512")
                             RowOf<float, Rec<P4608>, 4, 512, 3>::make("16.12.24r V4x512 paired l2pf"),
                             RowOf<float, P4608, 2, 256>::make("16.12.24 V2x256"),
                             RowOf<float, Rec<P4608>, 4, 576, 15>::make("16.12.24r V4x576 tma-in tma-out l2pf"),
-                            RowOf<float, Rec<P4608>, 2, 288, 31>::make("16.12.24r V2x288 tma-in tma-out l2pf")};
+                            RowOf<float, Rec<P4608>, 2, 288, 31>::make("16.12.24r V2x288 tma-in tma-out l2pf"),
+                            RowOf<float, Rec<P4608>, 2, 288, 30>::make("16.12.24r V2x288 tma-in tma-out")};
 const ColKernels c3072[] = {ColOf<float, P4608, 256>::make("16.12.24 x256"), ColOf<float, P4608, 512>::make("16.12.24 x512"),
                             ColOf<float, Rec<P4608>, 256>::make("16.12.24r x256"),
                             ColOf<float, Rec<P4608>, 256, 2>::make("16.12.24r x256 hoist")};

@@ -18,7 +18,8 @@ const RowKernels r384[] = {RowOf<float, P576, 4, 256>::make("24.24 V4x256"),
                            RowOf<float, Rec<P576>, 4, 256, 2>::make("24.24r V4x256 paired"),
                            RowOf<float, Rec<P576>, 4, 128, 15>::make("24.24r V4x128 tma-in tma-out l2pf"),
                            RowOf<float, Rec<P576>, 4, 256, 15>::make("24.24r V4x256 tma-in tma-out l2pf"),
-                           RowOf<float, Rec<P576b>, 4, 192, 15>::make("6.6.16r V4x192 tma-in tma-out l2pf")};
+                           RowOf<float, Rec<P576b>, 4, 192, 15>::make("6.6.16r V4x192 tma-in tma-out l2pf"),
+                           RowOf<float, Rec<P576b>, 4, 192, 14>::make("6.6.16r V4x192 tma-in tma-out")};
 const ColKernels c384[] = {ColOf<float, P576, 128>::make("24.24 x128"), ColOf<float, P576b, 128>::make("6.6.16 x128"),
                            ColOf<float, Rec<P576>, 128, 2>::make("24.24r x128 hoist")};
 const RowKernels r512[] = {RowOf<float, P768, 4, 256>::make("32.24 V4x256"),
@@ -28,7 +29,8 @@ const RowKernels r512[] = {RowOf<float, P768, 4, 256>::make("32.24 V4x256"),
                            RowOf<float, Rec<P768b>, 4, 256, 2>::make("16.2.24r V4x256 paired"),
                            RowOf<float, Rec<P768b>, 4, 128, 15>::make("16.2.24r V4x128 tma-in tma-out l2pf"),
                            RowOf<float, Rec<P768b>, 4, 256, 15>::make("16.2.24r V4x256 tma-in tma-out l2pf"),
-                           RowOf<float, Rec<P768>, 4, 128, 15>::make("32.24r V4x128 tma-in tma-out l2pf")};
+                           RowOf<float, Rec<P768>, 4, 128, 15>::make("32.24r V4x128 tma-in tma-out l2pf"),
+                           RowOf<float, Rec<P768b>, 4, 128, 14>::make("16.2.24r V4x128 tma-in tma-out")};
 const ColKernels c512[] = {ColOf<float, P768, 128>::make("32.24 x128"), ColOf<float, P768b, 128>::make("16.2.24 x128"),
                            ColOf<float, P768, 256>::make("32.24 x256"),
                            ColOf<float, Rec<P768>, 128, 2>::make("32.24r x128 hoist"),
@@ -37,7 +39,8 @@ const RowKernels r768[] = {RowOf<float, P1152, 4, 256>::make("8.6.24 V4x256"),
                            RowOf<float, P1152, 2, 256>::make("8.6.24 V2x256"),
                            RowOf<float, P1152b, 4, 256>::make("12.4.24 V4x256"),
                            RowOf<float, Rec<P1152>, 4, 288, 3>::make("8.6.24r V4x288 paired l2pf"),
-                           RowOf<float, Rec<P1152>, 4, 288, 15>::make("8.6.24r V4x288 tma-in tma-out l2pf")};
+                           RowOf<float, Rec<P1152>, 4, 288, 15>::make("8.6.24r V4x288 tma-in tma-out l2pf"),
+                           RowOf<float, Rec<P1152>, 4, 288, 14>::make("8.6.24r V4x288 tma-in tma-out")};
 const ColKernels c768[] = {ColOf<float, P1152, 256>::make("8.6.24 x256"), ColOf<float, P1152, 128>::make("8.6.24 x128"),
                            ColOf<float, P1152b, 256>::make("12.4.24 x256"),
                            ColOf<float, Rec<P1152>, 288, 3>::make("8.6.24r x288 hoist pipe0"),

@@ -15,7 +15,8 @@ const RowKernels r1024[] = {RowOf<float, P1536, 4, 256>::make("16.4.24 V4x256"),
                             RowOf<float, P1536b, 4, 256>::make("8.8.24 V4x256"),
                             RowOf<float, Rec<P1536>, 4, 192, 3>::make("16.4.24r V4x192 paired l2pf"),
                             RowOf<float, Rec<P1536>, 4, 256, 3>::make("16.4.24r V4x256 paired l2pf"),
-                            RowOf<float, Rec<P1536>, 4, 192, 31>::make("16.4.24r V4x192 tma-in tma-out l2pf")};
+                            RowOf<float, Rec<P1536>, 4, 192, 31>::make("16.4.24r V4x192 tma-in tma-out l2pf"),
+                            RowOf<float, Rec<P1536>, 4, 192, 30>::make("16.4.24r V4x192 tma-in tma-out")};
 const ColKernels c1024[] = {ColOf<float, P1536, 256>::make("16.4.24 x256"), ColOf<float, P1536, 128>::make("16.4.24 x128"),
                             ColOf<float, P1536b, 256>::make("8.8.24 x256"),
                             ColOf<float, Rec<P1536>, 128, 1>::make("16.4.24r x128 pref"),
@@ -26,7 +27,8 @@ const RowKernels r1536[] = {RowOf<float, P2304, 4, 512>::make("16.6.24 V4x512"),
                             RowOf<float, P2304, 2, 256>::make("16.6.24 V2x256"),
                             RowOf<float, Rec<P2304>, 4, 288, 3>::make("16.6.24r V4x288 paired l2pf"),
                             RowOf<float, Rec<P2304>, 4, 576, 3>::make("16.6.24r V4x576 paired l2pf"),
-                            RowOf<float, Rec<P2304>, 4, 288, 31>::make("16.6.24r V4x288 tma-in tma-out l2pf")};
+                            RowOf<float, Rec<P2304>, 4, 288, 31>::make("16.6.24r V4x288 tma-in tma-out l2pf"),
+                            RowOf<float, Rec<P2304>, 4, 288, 30>::make("16.6.24r V4x288 tma-in tma-out")};
 const ColKernels c1536[] = {ColOf<float, P2304, 256>::make("16.6.24 x256"), ColOf<float, P2304, 128>::make("16.6.24 x128"),
                             ColOf<float, Rec<P2304>, 288, 3>::make("16.6.24r x288 hoist pipe0"),
                             ColOf<float, Rec<P2304>, 256, 2>::make("16.6.24r x256 hoist")};

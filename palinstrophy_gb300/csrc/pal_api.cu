@@ -48,7 +48,8 @@ struct pal_handle {
   cudaStream_t stream = nullptr;
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr;
   void *om_p = nullptr, *fm_p = nullptr;  // om / fnm1 in butterfly-major order, used inside pal_step
-  pal::TmaMaps tmaps{};                   // w0 / w1 descriptors when the row candidate stores through TMA
+  pal::TmaMaps tmaps{};                   // w0 / w1 descriptors when the row candidate moves rows by TMA
+  pal::TmaMaps cmaps{};                   // w0 / w1 descriptors when the column candidate moves planes by TMA
   std::map<std::string, cudaGraphExec_t> step_graphs;  // pal_step sequences of small grids, by NEXTDT pattern
   void *tw_row = nullptr, *tw_col = nullptr;
   void *stage = nullptr, *phys = nullptr;
@@ -80,6 +81,34 @@ bool encode_row_maps(TmaMaps* out, void* w0, void* w1, int N, int V, int members
   const cuuint64_t dims[3] = {(cuuint64_t)2 * M, (cuuint64_t)Nh, (cuuint64_t)members};
   const cuuint64_t strides[2] = {(cuuint64_t)M * 8, (cuuint64_t)Nh * M * 8};  // bytes, dims 1 and 2
   const cuuint32_t box[3] = {(cuuint32_t)(2 * V), (cuuint32_t)tma_box_rows(Nh), 1};
+  const cuuint32_t elem[3] = {1, 1, 1};
+  void* base[2] = {w0, w1};
+  CUtensorMap* maps[2] = {&out->w0, &out->w1};
+  for (int i = 0; i < 2; ++i) {
+    CUresult r = encode(maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base[i], dims, strides, box, elem,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+  }
+  return true;
+}
+
+bool encode_col_maps(TmaMaps* out, void* w0, void* w1, int N, int RP, int members) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
+  const int M = 3 * N / 2, Nh = N / 2, G = M / RP;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * RP, (cuuint64_t)G, (cuuint64_t)Nh * members};
+  const cuuint64_t strides[2] = {(cuuint64_t)RP * 8, (cuuint64_t)M * 8};  // bytes, dims 1 and 2
+  // the box's inner extent (2 RP + 4 floats) runs past the 2 RP floats of a
+  // group: loads fill those 4 floats with zeros, stores leave them out
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * RP + 4), (cuuint32_t)(G < 256 ? G : 256), 1};
   const cuuint32_t elem[3] = {1, 1, 1};
   void* base[2] = {w0, w1};
   CUtensorMap* maps[2] = {&out->w0, &out->w1};
@@ -133,6 +162,7 @@ StepArgs base_args(pal_handle* h) {
   a.om_p = h->om_p;
   a.fm_p = h->fm_p;
   a.tmaps = &h->tmaps;
+  a.cmaps = &h->cmaps;
   a.N = h->N;
   return a;
 }
@@ -250,6 +280,8 @@ int select_variant(pal_handle* h, int row, int col) {
   h->ck = &h->ks->cols[col];
   if (h->rk->tma && !pal::encode_row_maps(&h->tmaps, h->w0, h->w1, h->N, h->rk->V, 1))
     return fail(h, PAL_ERR_CUDA, "TMA descriptor of the work planes could not be encoded");
+  if (h->ck->tma && !pal::encode_col_maps(&h->cmaps, h->w0, h->w1, h->N, h->ck->rp, 1))
+    return fail(h, PAL_ERR_CUDA, "TMA descriptor of the work planes (columns) could not be encoded");
   h->rk->twiddles(h->tw_row, h->stream);
   h->ck->twiddles(h->tw_col, h->stream);
   PAL_LAUNCHED(h, "twiddle tables");
@@ -412,7 +444,7 @@ int pal_create(int N, int precision, double Re, double cfl, pal_handle** out) {
   h->spectral_blocks = std::max(1, std::min(4 * sms, (int)(((size_t)N * h->Nh + 255) / 256)));
   const size_t part_n = (size_t)std::max(h->M, std::max(1024, h->spectral_blocks)) * 5;
   void** bufs[] = {&h->w0, &h->w1, &h->om, &h->fnm1, &h->stage, &h->tw_row, &h->tw_col, &h->om_p};
-  const size_t sizes[] = {plane_w,           plane_w,           plane_om, plane_om, 2 * plane_om,
+  const size_t sizes[] = {plane_w + pal::kPlaneSlack, plane_w + pal::kPlaneSlack, plane_om, plane_om, 2 * plane_om,
                           tw_max * h->esz, tw_max * h->esz, 2 * plane_w};
   for (int i = 0; i < 8; ++i) {
     e = cudaMalloc(bufs[i], sizes[i]);

@@ -41,6 +41,7 @@ struct Group {
   void *w0 = nullptr, *w1 = nullptr, *om = nullptr, *fnm1 = nullptr, *vel = nullptr;
   void *om_p = nullptr, *fm_p = nullptr;  // butterfly-major om / fnm1 used during pal_ensemble_step
   pal::TmaMaps tmaps{};                   // w0 / w1 descriptors (member dimension = group size)
+  pal::TmaMaps cmaps{};                   // the same for a column candidate that moves planes by TMA
   void *tw_row = nullptr, *tw_col = nullptr, *phys = nullptr;
   DevScalars* sc = nullptr;
   double* part = nullptr;
@@ -108,6 +109,7 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
   a.om_p = g.om_p;
   a.fm_p = g.fm_p;
   a.tmaps = &g.tmaps;
+  a.cmaps = &g.cmaps;
   a.N = g.N;
   a.members = (int)g.members.size();
   a.ms_w = (long long)g.Nh * g.M;
@@ -231,7 +233,7 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
     size_t tw_row_max = 0, tw_col_max = 0;  // room for any candidate's tables (pal_ensemble_autotune)
     for (int q = 0; q < g.ks->n_rows; ++q) tw_row_max = std::max(tw_row_max, (size_t)g.ks->rows[q].tw_elems);
     for (int q = 0; q < g.ks->n_cols; ++q) tw_col_max = std::max(tw_col_max, (size_t)g.ks->cols[q].tw_elems);
-    const size_t sizes[] = {nm * plane_w, nm * plane_w, nm * plane_om, nm * plane_om, 2 * nm * plane_om,
+    const size_t sizes[] = {nm * plane_w + pal::kPlaneSlack, nm * plane_w + pal::kPlaneSlack, nm * plane_om, nm * plane_om, 2 * nm * plane_om,
                             tw_row_max * e->esz, tw_col_max * e->esz, 2 * nm * plane_w};
     for (int i = 0; i < 8; ++i) {
       c = cudaMalloc(bufs[i], sizes[i]);
@@ -242,6 +244,8 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
     g.fm_p = static_cast<char*>(g.om_p) + nm * plane_w;
     if (g.rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, g.rk->V, (int)nm))
       return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble TMA descriptors"));
+    if (g.ck->tma && !pal::encode_col_maps(&g.cmaps, g.w0, g.w1, g.N, g.ck->rp, (int)nm))
+      return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble TMA descriptors (columns)"));
     c = cudaMalloc(&g.sc, nm * sizeof(DevScalars));
     if (c == cudaSuccess) c = cudaMalloc(&g.part, nm * g.part_stride * sizeof(double));
     if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_OOM, "ensemble scalars"));
@@ -358,6 +362,7 @@ int pal_ensemble_autotune(pal_ensemble* e) {
     for (int q = 0; q < g.ks->n_cols && rc == PAL_OK; ++q) {
       const pal::ColKernels* ck = &g.ks->cols[q];
       if (ck->configure() != cudaSuccess) continue;
+      if (ck->tma && !pal::encode_col_maps(&g.cmaps, g.w0, g.w1, g.N, ck->rp, nm)) continue;
       ck->twiddles(g.tw_col, e->stream);
       StepArgs a = group_args(e, g);
       a.tw = g.tw_col;
@@ -374,6 +379,10 @@ int pal_ensemble_autotune(pal_ensemble* e) {
     g.ck = best_c;
     if (g.rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, g.rk->V, nm)) {
       rc = efail(e, PAL_ERR_CUDA, "ensemble TMA descriptors");
+      break;
+    }
+    if (g.ck->tma && !pal::encode_col_maps(&g.cmaps, g.w0, g.w1, g.N, g.ck->rp, nm)) {
+      rc = efail(e, PAL_ERR_CUDA, "ensemble TMA descriptors (columns)");
       break;
     }
     g.rk->twiddles(g.tw_row, e->stream);

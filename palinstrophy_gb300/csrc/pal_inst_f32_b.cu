@@ -25,7 +25,8 @@ const ColKernels c2048[] = {ColOf<float, P3072, 256>::make("16.8.24 x256"), ColO
                             ColOf<float, Rec<P3072b>, 256, 1>::make("8.16.24r x256 pref"),
                             ColOf<float, Rec<P3072b>, 512, 1>::make("8.16.24r x512 pref"),
                             ColOf<float, Rec<P3072b>, 256, 2>::make("8.16.24r x256 hoist"),
-                            ColOf<float, Rec<P3072b>, 256, 3>::make("8.16.24r x256 hoist pipe0")};
+                            ColOf<float, Rec<P3072b>, 256, 3>::make("8.16.24r x256 hoist pipe0"),
+                            ColOf<float, Rec<P3072b>, 256, 4>::make("8.16.24r x256 tma")};
 const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512"),
                             RowOf<float, Rec<P4608>, 4, 576, 3>::make("16.12.24r V4x576 paired l2pf"),
                             RowOf<float, Rec<P4608>, 4, 512, 3>::make("16.12.24r V4x512 paired l2pf"),
@@ -35,7 +36,8 @@ const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512")
                             RowOf<float, Rec<P4608>, 2, 288, 30>::make("16.12.24r V2x288 tma-in tma-out")};
 const ColKernels c3072[] = {ColOf<float, P4608, 256>::make("16.12.24 x256"), ColOf<float, P4608, 512>::make("16.12.24 x512"),
                             ColOf<float, Rec<P4608>, 256>::make("16.12.24r x256"),
-                            ColOf<float, Rec<P4608>, 256, 2>::make("16.12.24r x256 hoist")};
+                            ColOf<float, Rec<P4608>, 256, 2>::make("16.12.24r x256 hoist"),
+                            ColOf<float, Rec<P4608>, 256, 4>::make("16.12.24r x256 tma")};
 
 PAL_KERNEL_SET(float, 0, 2048, r2048, c2048)
 PAL_KERNEL_SET(float, 0, 3072, r3072, c3072)

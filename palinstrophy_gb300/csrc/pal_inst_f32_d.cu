@@ -20,7 +20,8 @@ const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
                             ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),
                             ColOf<float, Rec<P12288>, 512, 3>::make("16.32.24r x512 hoist pipe0"),
-                            ColOf<float, RecT<P12288>, 512, 3>::make("16.32.24t x512 hoist pipe0")};
+                            ColOf<float, RecT<P12288>, 512, 3>::make("16.32.24t x512 hoist pipe0"),
+                            ColOf<float, Rec<P12288>, 512, 4>::make("16.32.24r x512 tma")};
 
 PAL_KERNEL_SET(float, 0, 8192, r8192, c8192)
 }  // namespace

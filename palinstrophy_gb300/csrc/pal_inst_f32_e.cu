@@ -34,7 +34,8 @@ const RowKernels r512[] = {RowOf<float, P768, 4, 256>::make("32.24 V4x256"),
 const ColKernels c512[] = {ColOf<float, P768, 128>::make("32.24 x128"), ColOf<float, P768b, 128>::make("16.2.24 x128"),
                            ColOf<float, P768, 256>::make("32.24 x256"),
                            ColOf<float, Rec<P768>, 128, 2>::make("32.24r x128 hoist"),
-                           ColOf<float, Rec<P768b>, 128, 2>::make("16.2.24r x128 hoist")};
+                           ColOf<float, Rec<P768b>, 128, 2>::make("16.2.24r x128 hoist"),
+                           ColOf<float, Rec<P768b>, 128, 4>::make("16.2.24r x128 tma")};
 const RowKernels r768[] = {RowOf<float, P1152, 4, 256>::make("8.6.24 V4x256"),
                            RowOf<float, P1152, 2, 256>::make("8.6.24 V2x256"),
                            RowOf<float, P1152b, 4, 256>::make("12.4.24 V4x256"),
@@ -44,7 +45,8 @@ const RowKernels r768[] = {RowOf<float, P1152, 4, 256>::make("8.6.24 V4x256"),
 const ColKernels c768[] = {ColOf<float, P1152, 256>::make("8.6.24 x256"), ColOf<float, P1152, 128>::make("8.6.24 x128"),
                            ColOf<float, P1152b, 256>::make("12.4.24 x256"),
                            ColOf<float, Rec<P1152>, 288, 3>::make("8.6.24r x288 hoist pipe0"),
-                           ColOf<float, Rec<P1152>, 256, 2>::make("8.6.24r x256 hoist")};
+                           ColOf<float, Rec<P1152>, 256, 2>::make("8.6.24r x256 hoist"),
+                           ColOf<float, Rec<P1152>, 256, 4>::make("8.6.24r x256 tma")};
 
 PAL_KERNEL_SET(float, 0, 384, r384, c384)
 PAL_KERNEL_SET_ADJ(float, 0, 512, r512, c512, (AdjOf<float, P768, 4, 256, P768, 128>::get()))

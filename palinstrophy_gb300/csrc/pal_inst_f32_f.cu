@@ -22,7 +22,8 @@ const ColKernels c1024[] = {ColOf<float, P1536, 256>::make("16.4.24 x256"), ColO
                             ColOf<float, Rec<P1536>, 128, 1>::make("16.4.24r x128 pref"),
                             ColOf<float, Rec<P1536>, 256, 1>::make("16.4.24r x256 pref"),
                             ColOf<float, Rec<P1536>, 192, 3>::make("16.4.24r x192 hoist pipe0"),
-                            ColOf<float, Rec<P1536>, 256, 2>::make("16.4.24r x256 hoist")};
+                            ColOf<float, Rec<P1536>, 256, 2>::make("16.4.24r x256 hoist"),
+                            ColOf<float, Rec<P1536>, 128, 4>::make("16.4.24r x128 tma")};
 const RowKernels r1536[] = {RowOf<float, P2304, 4, 512>::make("16.6.24 V4x512"),
                             RowOf<float, P2304, 2, 256>::make("16.6.24 V2x256"),
                             RowOf<float, Rec<P2304>, 4, 288, 3>::make("16.6.24r V4x288 paired l2pf"),
@@ -31,7 +32,8 @@ const RowKernels r1536[] = {RowOf<float, P2304, 4, 512>::make("16.6.24 V4x512"),
                             RowOf<float, Rec<P2304>, 4, 288, 30>::make("16.6.24r V4x288 tma-in tma-out")};
 const ColKernels c1536[] = {ColOf<float, P2304, 256>::make("16.6.24 x256"), ColOf<float, P2304, 128>::make("16.6.24 x128"),
                             ColOf<float, Rec<P2304>, 288, 3>::make("16.6.24r x288 hoist pipe0"),
-                            ColOf<float, Rec<P2304>, 256, 2>::make("16.6.24r x256 hoist")};
+                            ColOf<float, Rec<P2304>, 256, 2>::make("16.6.24r x256 hoist"),
+                            ColOf<float, Rec<P2304>, 256, 4>::make("16.6.24r x256 tma")};
 PAL_KERNEL_SET(float, 0, 1024, r1024, c1024)
 PAL_KERNEL_SET(float, 0, 1536, r1536, c1536)
 }  // namespace

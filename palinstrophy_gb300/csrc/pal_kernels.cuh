@@ -73,7 +73,8 @@ struct StepArgs {
   int ahead;        // resident blocks of one wave (L2-prefetch candidates; 0 = none)
   void* om_p;       // om / fnm1 in the column plan's butterfly-major order (N/2 x M)
   void* fm_p;
-  const struct TmaMaps* tmaps;  // host: descriptors of w0 / w1 for the row pass's bulk stores
+  const struct TmaMaps* tmaps;  // host: descriptors of w0 / w1 for the row pass's bulk copies
+  const struct TmaMaps* cmaps;  // host: descriptors of w0 / w1 for the column pass's bulk copies
 };
 
 // Rows per TMA box of the row tiles: the largest power of two up to 256 that
@@ -284,6 +285,22 @@ __device__ __forceinline__ void tma_load_3d(const CUtensorMap* map, void* smem, 
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(d),
       "l"(map), "r"(b), "r"(x), "r"(y), "r"(z)
       : "memory");
+}
+// Wait for phase `parity` of the mbarrier with non-blocking polls
+// (mbarrier.test_wait), giving up after max_iter of them: a bound in time even
+// if the expected transaction count were never reached.
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long* bar, unsigned parity, int max_iter) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  for (int i = 0; i < max_iter; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
 }
 // Wait for phase `parity` of the mbarrier, giving up after max_iter polls.
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int max_iter) {
@@ -811,6 +828,24 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
   return cf;
 }
 
+// Planar column tile for bulk tensor copies: plane v (A / u^, B / v^) starts at
+// v * PB; within a plane, position k sits at k + 2 (k / RP), i.e. every RP
+// positions (RP complex = 48 floats) are followed by 2 pad slots.  A group of
+// RP + 2 slots is then one 52-float row of a TMA box over a 48-float tensor
+// dimension: loads fill the pads with zeros and stores skip them.  The plane
+// stride keeps both planes 128-byte aligned.
+template <class PL>
+struct ColPlanar {
+  static constexpr int RP = PL::RP;
+  static constexpr int PADM = PL::M + 2 * (PL::M / RP);         // slots per plane
+  static constexpr int PB = ((PADM * 8 + 127) / 128) * 128 / 8;  // plane stride (FP32 complex)
+  static constexpr int G = PL::M / RP;                          // groups per plane
+  static constexpr int GBOX = G < 256 ? G : 256;                // groups per TMA box
+  static __device__ __forceinline__ int phys(int k) { return k + 2 * (k / RP); }
+  static constexpr int pstride(int p) { return PL::stride(p) == 1 ? 1 : PL::stride(p) + 2 * (PL::stride(p) / RP); }
+  static constexpr bool fits = PL::M % RP == 0 && G % GBOX == 0 && (2 * RP + 4) * 4 % 16 == 0;  // whole groups, boxes
+};
+
 // Middle of the column pass: last forward DIF -> nonlinear term, update,
 // inversion -> first inverse DIT.  The two lanes of a butterfly hold A and B;
 // lane 0 updates the even positions and lane 1 the odd ones, trading operands
@@ -832,7 +867,12 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
 // whose c3 is 0.  The last stage stores om and fn as the reference state.
 // QM: the F_Q_* / F_NO_FM_IN flags are honoured (a separate instantiation, so
 // that the plain update keeps its register budget).
-template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false, bool QM = false>
+//
+// PLANAR: the tile is ColPlanar's two padded planes instead of the
+// interleaved [slot][v] layout; half-warps hold one plane (lane bit 4), so the
+// two planes of a butterfly trade operands across lanes 16 apart.
+template <typename T, class PL, int NT, bool SMEM_OM, bool PERM, bool HOIST = false, bool QM = false,
+          bool PLANAR = false>
 __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, const cplx<T>* s_fm,
                                            cplx<T>* __restrict__ om, cplx<T>* __restrict__ fm,
                                            const ModeCoef<T>& cf, int kx, int tid, int flags) {
@@ -848,12 +888,18 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
   constexpr int FSTEP = M / R;
   constexpr bool BAND_CT = (R % 3 == 0) && ((R / 3) % 2 == 0);
   const T ax = T(kx);
+  constexpr int ES = PLANAR ? 1 : V;           // element stride of a butterfly in the tile
+  constexpr int XL = PLANAR ? 16 : 1;          // lane distance between the two planes
   for (int w0i = 0; w0i < NB; w0i += NT) {
     const int w = w0i + tid;
     const bool act = w < NB;
-    const int v = w & 1;
-    const int b = act ? (w >> 1) : 0;
-    C* p = sm + b * (R + 1) * V + v;
+    const int v = PLANAR ? ((w >> 4) & 1) : (w & 1);
+    const int b = act ? (PLANAR ? (((w >> 5) << 4) | (w & 15)) : (w >> 1)) : 0;
+    C* p;
+    if constexpr (PLANAR)
+      p = sm + v * ColPlanar<PL>::PB + b * (R + 2);
+    else
+      p = sm + b * (R + 1) * V + v;
     const int fb = PL::freq(b * R);
     constexpr int NH = HOIST ? R / 2 : 1;
     C h_o[NH], h_f[NH];
@@ -874,7 +920,7 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
     }
     C x[R];
 #pragma unroll
-    for (int j = 0; j < R; ++j) x[j] = act ? p[j * V] : C{T(0), T(0)};
+    for (int j = 0; j < R; ++j) x[j] = act ? p[j * ES] : C{T(0), T(0)};
     Dft<R, -1, C>::run(x);
 #pragma unroll
     for (int j = 0; j < R; j += 2) {
@@ -886,8 +932,8 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       // lane 0 takes position j, lane 1 position j+1
       const C send = v == 0 ? x[j + 1] : x[j];
       C recv;
-      recv.x = __shfl_xor_sync(0xffffffffu, send.x, 1);
-      recv.y = __shfl_xor_sync(0xffffffffu, send.y, 1);
+      recv.x = __shfl_xor_sync(0xffffffffu, send.x, XL);
+      recv.y = __shfl_xor_sync(0xffffffffu, send.y, XL);
       const C Az = v == 0 ? x[j] : recv;
       const C Bz = v == 0 ? recv : x[j + 1];
       const int f = fb + (j + v) * FSTEP;
@@ -938,15 +984,15 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       // lane 0 keeps u^ of position j and receives u^ of j+1; lane 1 the v^ pair
       const C send2 = v == 0 ? vh : uh;
       C recv2;
-      recv2.x = __shfl_xor_sync(0xffffffffu, send2.x, 1);
-      recv2.y = __shfl_xor_sync(0xffffffffu, send2.y, 1);
+      recv2.x = __shfl_xor_sync(0xffffffffu, send2.x, XL);
+      recv2.y = __shfl_xor_sync(0xffffffffu, send2.y, XL);
       x[j] = v == 0 ? uh : recv2;
       x[j + 1] = v == 0 ? recv2 : vh;
     }
     Dft<R, +1, C>::run(x);
     if (act) {
 #pragma unroll
-      for (int j = 0; j < R; ++j) p[j * V] = x[j];
+      for (int j = 0; j < R; ++j) p[j * ES] = x[j];
     }
   }
   __syncthreads();
@@ -1089,6 +1135,118 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
                                                                              tid, a.flags);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
+  col_finish<NT>(a, tid);
+}
+
+// One DIF (DIT = false) or DIT pass over a planar column tile (ColPlanar):
+// item w is butterfly ((w >> 5) << 4) | (w & 15) of plane (w >> 4) & 1, so a
+// half-warp reads 16 consecutive butterflies of one plane.  The arithmetic is
+// dif_pass / dit_pass's; only the addressing differs.
+template <typename T, class PL, int NT, int P, int SIGN, bool DIT>
+__device__ __forceinline__ void col_pass_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  using C = cplx<T>;
+  using CP = ColPlanar<PL>;
+  constexpr int R = PL::R[P];
+  constexpr int L = PL::span(P);
+  constexpr int S = L / R;
+  constexpr int SP = CP::pstride(P);
+  constexpr int NB = 2 * (PL::M / R);
+  static_assert((PL::M / R) % 16 == 0 && NT % 32 == 0, "whole half-warps per plane");
+  static_assert(S == 1 || S % CP::RP == 0, "strides other than the last are whole pad groups");
+  for (int w = tid; w < NB; w += NT) {
+    const int v = (w >> 4) & 1;
+    const int b = ((w >> 5) << 4) | (w & 15);
+    const int blk = b / S;
+    const int i = b - blk * S;
+    C* p = sm + v * CP::PB + CP::phys(blk * L + i);
+    C x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = p[k * SP];
+    if constexpr (DIT) {
+      if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
+      Dft<R, SIGN, C>::run(x);
+    } else {
+      Dft<R, SIGN, C>::run(x);
+      if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) p[k * SP] = x[k];
+  }
+}
+// DIF passes P .. TO-1, DIT passes P down to TO, each followed by a barrier.
+template <typename T, class PL, int NT, int SIGN, int P, int TO>
+__device__ __forceinline__ void col_dif_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  if constexpr (P < TO) {
+    col_pass_planar<T, PL, NT, P, SIGN, false>(sm, tw, tid);
+    __syncthreads();
+    col_dif_planar<T, PL, NT, SIGN, P + 1, TO>(sm, tw, tid);
+  }
+}
+template <typename T, class PL, int NT, int SIGN, int P, int TO>
+__device__ __forceinline__ void col_dit_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  if constexpr (P >= TO) {
+    col_pass_planar<T, PL, NT, P, SIGN, true>(sm, tw, tid);
+    __syncthreads();
+    col_dit_planar<T, PL, NT, SIGN, P - 1, TO>(sm, tw, tid);
+  }
+}
+
+// k_col with the column moved by the TMA unit: one elected thread loads both
+// P-state planes of column kx (groups of RP complex into ColPlanar's padded
+// rows, zero-filled pads) with 3D bulk tensor loads completing on one
+// mbarrier, every pass runs in place in shared memory (the first forward DIF
+// pass and the last inverse DIT pass included), and the U-state planes leave
+// by bulk tensor stores that skip the pads.  om / fnm1 are the butterfly-major
+// columns (om_p, fm_p), read and written by the lanes as in k_col.  Same
+// arithmetic as k_col, so the same results bit for bit.  FP32.
+template <typename T, class PL, int NT, bool QM>
+__global__ void __launch_bounds__(NT) k_col_tma(StepArgs a0, const __grid_constant__ TmaMaps maps) {
+  using C = cplx<T>;
+  using CP = ColPlanar<PL>;
+  static_assert(sizeof(C) == 8 && CP::fits, "FP32 planes of whole pad groups and boxes");
+  const StepArgs a = member_args(a0, sizeof(C));
+  extern __shared__ __align__(128) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  constexpr int M = PL::M;
+  constexpr int N = 2 * M / 3;
+  const int tid = threadIdx.x;
+  const int kx = blockIdx.x;
+  const int row = (int)blockIdx.y * (N / 2) + kx;  // the plane row of this column in the 3D view
+  const C* __restrict__ tw = static_cast<const C*>(a.tw);
+  C* __restrict__ om = static_cast<C*>(a.om_p) + (size_t)kx * M;
+  C* __restrict__ fm = static_cast<C*>(a.fm_p) + (size_t)kx * M;
+  __shared__ __align__(8) unsigned long long bar;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, 2u * CP::G * (2 * CP::RP + 4) * 4u);
+#pragma unroll 1
+    for (int g = 0; g < CP::G; g += CP::GBOX) {
+      tma_load_3d(&maps.w0, sm + g * (CP::RP + 2), &bar, 0, g, row);
+      tma_load_3d(&maps.w1, sm + CP::PB + g * (CP::RP + 2), &bar, 0, g, row);
+    }
+  }
+  const ModeCoef<T> cf = col_coef<T>(a, N);
+  __syncthreads();  // every thread sees the initialised barrier
+  if (!mbar_test_wait(&bar, 0, 1 << 20)) {
+    // the copies did not complete in time: report it and wait (bounded) for them
+    // before the shared memory is used or released
+    if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
+    mbar_test_wait(&bar, 0, 1 << 20);
+  }
+  col_dif_planar<T, PL, NT, -1, 0, PL::NP - 1>(sm, tw, tid);
+  col_middle<T, PL, NT, false, true, true, QM, true>(sm, nullptr, nullptr, om, fm, cf, kx, tid, a.flags);
+  col_dit_planar<T, PL, NT, +1, PL::NP - 2, 0>(sm, tw, tid);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+#pragma unroll 1
+    for (int g = 0; g < CP::G; g += CP::GBOX) {
+      tma_store_3d(&maps.w0, sm + g * (CP::RP + 2), 0, g, row);
+      tma_store_3d(&maps.w1, sm + CP::PB + g * (CP::RP + 2), 0, g, row);
+    }
+    tma_commit();
+    tma_wait_read();  // the shared memory stays the block's until the engine has read it
+  }
   col_finish<NT>(a, tid);
 }
 

@@ -40,6 +40,8 @@ struct ColKernels {
   void (*to_perm)(const StepArgs&, cudaStream_t);
   void (*from_perm)(const StepArgs&, cudaStream_t);
   int (*blocks_per_sm)();  // resident k_col blocks per SM (occupancy calculator)
+  bool tma;                // the butterfly-major pass moves its planes by TMA: the launch needs StepArgs::cmaps
+  int rp;                  // last radix of the plan (pad groups of the TMA column tile)
 };
 
 // Adjoint of one LS-IMEX-RK3 stage (pal_adjoint.cuh), on fixed plans.
@@ -75,11 +77,19 @@ struct KernelSet {
 constexpr int kSpectralThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;
 constexpr size_t kLargeTile = 64 * 1024;  // tiles from this size on ask for the max shared carveout
+// Bytes allocated after each work plane: the column pass's bulk tensor boxes
+// reach 16 bytes past the last group of a row (ColPlanar), and this keeps
+// every such byte inside the allocation.
+constexpr size_t kPlaneSlack = 256;
 
 // TMA descriptors of the planes w0 / w1 (members x N/2 rows x M complex FP32)
 // for a row candidate with tile height V; false if the driver call is missing
 // or refuses the layout.
 bool encode_row_maps(TmaMaps* out, void* w0, void* w1, int N, int V, int members);
+// Descriptors of w0 / w1 for k_col_tma: each a 3D view (2 RP floats, M / RP
+// groups, N/2 x members rows) with a (2 RP + 4 floats, min(256, M / RP), 1)
+// box, so one box row is a padded group of ColPlanar.
+bool encode_col_maps(TmaMaps* out, void* w0, void* w1, int N, int RP, int members);
 
 template <typename T, class PL>
 void launch_twiddles(void* tw, cudaStream_t s) {
@@ -148,15 +158,32 @@ struct RowOf {
 
 template <typename T, class PL, int NT, int PREF = 0>
 struct ColOf {
+  // PREF 4: the butterfly-major pass is k_col_tma (planar tile, TMA bulk
+  // copies of the planes); the natural-order pass is the plain k_col
+  static constexpr bool TMA = PREF == 4;
+  static constexpr int BASE = TMA ? 0 : PREF;
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
-  static constexpr size_t smem = smem_inv + (PREF == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
+  static constexpr size_t smem = smem_inv + (BASE == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   // the butterfly-major variant has no shared-memory om staging (PREF 1)
-  static constexpr int PERM_PREF = PREF == 1 ? 0 : PREF;
-  static_assert(smem <= kSmemLimit, "column tile does not fit in shared memory");
+  static constexpr int PERM_PREF = BASE == 1 ? 0 : BASE;
+  static constexpr size_t smem_tma = TMA ? size_t(2) * ColPlanar<PL>::PB * sizeof(cplx<T>) : 0;
+  static_assert(smem <= kSmemLimit && smem_tma <= kSmemLimit, "column tile does not fit in shared memory");
   static cudaError_t configure() {
     cudaError_t e =
-        cudaFuncSetAttribute(k_col<T, PL, NT, PREF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_col<T, PL, NT, BASE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    if constexpr (TMA) {
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+    }
     e = cudaFuncSetAttribute(k_col<T, PL, NT, PERM_PREF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_inv);
     if (e != cudaSuccess) return e;
@@ -178,10 +205,19 @@ struct ColOf {
     return cudaFuncSetAttribute(k_col_inv<T, PL, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_inv);
   }
   static dim3 grid(const StepArgs& a) { return dim3(a.N / 2, a.members > 1 ? a.members : 1); }
-  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, PREF, false><<<grid(a), NT, smem, s>>>(a); }
+  static void col(const StepArgs& a, cudaStream_t s) { k_col<T, PL, NT, BASE, false><<<grid(a), NT, smem, s>>>(a); }
   // RK3 stages carrying the combined term run the flag-aware instantiation;
   // every other butterfly-major column pass runs the plain update
   static void col_perm(const StepArgs& a, cudaStream_t s) {
+    if constexpr (TMA) {
+      static const TmaMaps none{};
+      const TmaMaps& m = a.cmaps ? *a.cmaps : none;
+      if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
+        k_col_tma<T, PL, NT, true><<<grid(a), NT, smem_tma, s>>>(a, m);
+      else
+        k_col_tma<T, PL, NT, false><<<grid(a), NT, smem_tma, s>>>(a, m);
+      return;
+    }
     if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
       k_col<T, PL, NT, PERM_PREF, true, true><<<grid(a), NT, smem_inv, s>>>(a);
     else
@@ -200,14 +236,16 @@ struct ColOf {
   }
   static int blocks_per_sm() {
     int n = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true, false>, NT, smem_inv) ==
-                   cudaSuccess
-               ? n
-               : -1;
+    cudaError_t e;
+    if constexpr (TMA)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col_tma<T, PL, NT, false>, NT, smem_tma);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true, false>, NT, smem_inv);
+    return e == cudaSuccess ? n : -1;
   }
   static constexpr ColKernels make(const char* name) {
     return ColKernels{name,    NT,     smem,     PL::TW_TOTAL,          configure, col,
-                      col_inv, launch_twiddles<T, PL>, col_perm, to_perm, from_perm, blocks_per_sm};
+                      col_inv, launch_twiddles<T, PL>, col_perm, to_perm, from_perm, blocks_per_sm, TMA, PL::RP};
   }
 };
 

@@ -919,8 +919,18 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
       }
     }
     C x[R];
+    if constexpr (PLANAR && sizeof(C) == 8) {
+      // a planar butterfly is R contiguous, 16-byte aligned slots: pairs by 128-bit loads
 #pragma unroll
-    for (int j = 0; j < R; ++j) x[j] = act ? p[j * ES] : C{T(0), T(0)};
+      for (int j = 0; j < R; j += 2) {
+        const float4 t = act ? reinterpret_cast<const float4*>(p)[j / 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        x[j] = C{t.x, t.y};
+        x[j + 1] = C{t.z, t.w};
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < R; ++j) x[j] = act ? p[j * ES] : C{T(0), T(0)};
+    }
     Dft<R, -1, C>::run(x);
 #pragma unroll
     for (int j = 0; j < R; j += 2) {
@@ -991,8 +1001,14 @@ __device__ __forceinline__ void col_middle(cplx<T>* sm, const cplx<T>* s_om, con
     }
     Dft<R, +1, C>::run(x);
     if (act) {
+      if constexpr (PLANAR && sizeof(C) == 8) {
 #pragma unroll
-      for (int j = 0; j < R; ++j) p[j * ES] = x[j];
+        for (int j = 0; j < R; j += 2)
+          reinterpret_cast<float4*>(p)[j / 2] = make_float4(x[j].x, x[j].y, x[j + 1].x, x[j + 1].y);
+      } else {
+#pragma unroll
+        for (int j = 0; j < R; ++j) p[j * ES] = x[j];
+      }
     }
   }
   __syncthreads();

@@ -507,3 +507,36 @@ def test_two_row_tiles_share_an_sm(ts):
             assert w["row_blocks_per_sm"] == 2, w["desc"]
     assert seen >= 2
     F.close()
+
+
+def test_tma_column_pass_equals_per_lane_column_pass(ts):
+    """The column pass that moves its planes by TMA into a planar padded tile
+    (`... tma`) does the per-lane kernel's arithmetic in the same order, so on
+    the same plan and block size the fields agree bit for bit."""
+    from palinstrophy_gb300 import _lib as L
+    N = 1024
+    if not L.supported(N, "fp32"):
+        pytest.skip("fp32 is not compiled for N=1024")
+    om2, uc, st = L.pao_generate(N, 12.0, 1e4, 5, "KM3")
+    F = ts.Field(N, "fp32", 1e4, 0.3)
+    v = F.variant()
+    cols = {}
+    for c in range(v["n_cols"]):
+        F.set_variant(v["row"], c)
+        cols[F.variant()["desc"].split("col[")[1].rstrip("]")] = c
+    assert "16.4.24r x128 tma" in cols and "16.4.24r x128 pref" in cols
+    out = []
+    for name in ("16.4.24r x128 pref", "16.4.24r x128 tma"):
+        F.set_variant(v["row"], cols[name])
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.step2a()
+        F.set_scalar("dt", 0.3 / (F.compute_cflm() * math.pi))
+        F.set_scalar("cn", 1.0)
+        F.set_scalar("cnm1", 0.0)
+        for method in ("LS_IMEX_RK3", "CNAB2"):
+            F.step(method, 3, update=0)
+        out.append((F.om2(), F.fnm1()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    F.close()

@@ -26,7 +26,8 @@ const ColKernels c2048[] = {ColOf<float, P3072, 256>::make("16.8.24 x256"), ColO
                             ColOf<float, Rec<P3072b>, 512, 1>::make("8.16.24r x512 pref"),
                             ColOf<float, Rec<P3072b>, 256, 2>::make("8.16.24r x256 hoist"),
                             ColOf<float, Rec<P3072b>, 256, 3>::make("8.16.24r x256 hoist pipe0"),
-                            ColOf<float, Rec<P3072b>, 256, 4>::make("8.16.24r x256 tma")};
+                            ColOf<float, Rec<P3072b>, 256, 4>::make("8.16.24r x256 tma"),
+                            ColOf<float, Rec<P3072b>, 256, 5>::make("8.16.24r x256 tma occ")};
 const RowKernels r3072[] = {RowOf<float, P4608, 4, 512>::make("16.12.24 V4x512"),
                             RowOf<float, Rec<P4608>, 4, 576, 3>::make("16.12.24r V4x576 paired l2pf"),
                             RowOf<float, Rec<P4608>, 4, 512, 3>::make("16.12.24r V4x512 paired l2pf"),

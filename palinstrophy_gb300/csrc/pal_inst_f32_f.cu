@@ -33,7 +33,8 @@ const RowKernels r1536[] = {RowOf<float, P2304, 4, 512>::make("16.6.24 V4x512"),
 const ColKernels c1536[] = {ColOf<float, P2304, 256>::make("16.6.24 x256"), ColOf<float, P2304, 128>::make("16.6.24 x128"),
                             ColOf<float, Rec<P2304>, 288, 3>::make("16.6.24r x288 hoist pipe0"),
                             ColOf<float, Rec<P2304>, 256, 2>::make("16.6.24r x256 hoist"),
-                            ColOf<float, Rec<P2304>, 256, 4>::make("16.6.24r x256 tma")};
+                            ColOf<float, Rec<P2304>, 256, 4>::make("16.6.24r x256 tma"),
+                            ColOf<float, Rec<P2304>, 256, 5>::make("16.6.24r x256 tma occ")};
 PAL_KERNEL_SET(float, 0, 1024, r1024, c1024)
 PAL_KERNEL_SET(float, 0, 1536, r1536, c1536)
 }  // namespace

@@ -1215,8 +1215,9 @@ __device__ __forceinline__ void col_dit_planar(cplx<T>* sm, const cplx<T>* __res
 // by bulk tensor stores that skip the pads.  om / fnm1 are the butterfly-major
 // columns (om_p, fm_p), read and written by the lanes as in k_col.  Same
 // arithmetic as k_col, so the same results bit for bit.  FP32.
-template <typename T, class PL, int NT, bool QM>
-__global__ void __launch_bounds__(NT) k_col_tma(StepArgs a0, const __grid_constant__ TmaMaps maps) {
+// MINB > 0 caps the registers so that MINB blocks share an SM.
+template <typename T, class PL, int NT, bool QM, int MINB = 0>
+__global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = cplx<T>;
   using CP = ColPlanar<PL>;
   static_assert(sizeof(C) == 8 && CP::fits, "FP32 planes of whole pad groups and boxes");

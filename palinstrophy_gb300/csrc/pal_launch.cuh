@@ -159,28 +159,32 @@ struct RowOf {
 template <typename T, class PL, int NT, int PREF = 0>
 struct ColOf {
   // PREF 4: the butterfly-major pass is k_col_tma (planar tile, TMA bulk
-  // copies of the planes); the natural-order pass is the plain k_col
-  static constexpr bool TMA = PREF == 4;
+  // copies of the planes); the natural-order pass is the plain k_col.
+  // PREF 5: the same with registers capped for three blocks per SM (tiles of
+  // at most a third of the shared memory).
+  static constexpr bool TMA = PREF == 4 || PREF == 5;
   static constexpr int BASE = TMA ? 0 : PREF;
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
   static constexpr size_t smem = smem_inv + (BASE == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   // the butterfly-major variant has no shared-memory om staging (PREF 1)
   static constexpr int PERM_PREF = BASE == 1 ? 0 : BASE;
   static constexpr size_t smem_tma = TMA ? size_t(2) * ColPlanar<PL>::PB * sizeof(cplx<T>) : 0;
+  static constexpr int MINB = PREF == 5 ? 3 : 0;
+  static_assert(PREF != 5 || 3 * (smem_tma + 1024 + 256) <= size_t(228 * 1024), "three tiles per SM");
   static_assert(smem <= kSmemLimit && smem_tma <= kSmemLimit, "column tile does not fit in shared memory");
   static cudaError_t configure() {
     cudaError_t e =
         cudaFuncSetAttribute(k_col<T, PL, NT, BASE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if constexpr (TMA) {
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
     }
@@ -213,9 +217,9 @@ struct ColOf {
       static const TmaMaps none{};
       const TmaMaps& m = a.cmaps ? *a.cmaps : none;
       if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
-        k_col_tma<T, PL, NT, true><<<grid(a), NT, smem_tma, s>>>(a, m);
+        k_col_tma<T, PL, NT, true, MINB><<<grid(a), NT, smem_tma, s>>>(a, m);
       else
-        k_col_tma<T, PL, NT, false><<<grid(a), NT, smem_tma, s>>>(a, m);
+        k_col_tma<T, PL, NT, false, MINB><<<grid(a), NT, smem_tma, s>>>(a, m);
       return;
     }
     if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
@@ -238,7 +242,7 @@ struct ColOf {
     int n = 0;
     cudaError_t e;
     if constexpr (TMA)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col_tma<T, PL, NT, false>, NT, smem_tma);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col_tma<T, PL, NT, false, MINB>, NT, smem_tma);
     else
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true, false>, NT, smem_inv);
     return e == cudaSuccess ? n : -1;

@@ -160,17 +160,16 @@ template <typename T, class PL, int NT, int PREF = 0>
 struct ColOf {
   // PREF 4: the butterfly-major pass is k_col_tma (planar tile, TMA bulk
   // copies of the planes); the natural-order pass is the plain k_col.
-  // PREF 5: the same with registers capped for three blocks per SM (tiles of
-  // at most a third of the shared memory).
-  static constexpr bool TMA = PREF == 4 || PREF == 5;
+  // PREF 5 / 6: the same with registers capped for three / two blocks per SM.
+  static constexpr bool TMA = PREF == 4 || PREF == 5 || PREF == 6;
   static constexpr int BASE = TMA ? 0 : PREF;
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
   static constexpr size_t smem = smem_inv + (BASE == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
   // the butterfly-major variant has no shared-memory om staging (PREF 1)
   static constexpr int PERM_PREF = BASE == 1 ? 0 : BASE;
   static constexpr size_t smem_tma = TMA ? size_t(2) * ColPlanar<PL>::PB * sizeof(cplx<T>) : 0;
-  static constexpr int MINB = PREF == 5 ? 3 : 0;
-  static_assert(PREF != 5 || 3 * (smem_tma + 1024 + 256) <= size_t(228 * 1024), "three tiles per SM");
+  static constexpr int MINB = PREF == 5 ? 3 : PREF == 6 ? 2 : 0;
+  static_assert(MINB * (smem_tma + 1024 + 256) <= size_t(228 * 1024), "the capped block count fits in shared memory");
   static_assert(smem <= kSmemLimit && smem_tma <= kSmemLimit, "column tile does not fit in shared memory");
   static cudaError_t configure() {
     cudaError_t e =

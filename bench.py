@@ -24,8 +24,14 @@ Printed JSON line (rank 0):
 
 --impl reference times the reference's CPU implementation of the path (its FP32
 NumPy/scipy.fft step, restated operation for operation in oracle/ because the
-Python reference cannot be installed on the GPU host) on the same workload,
-with all host threads, for a bounded number of steps.
+Python reference cannot be installed on the GPU host) on the same workload from
+the reference generator's field (restated in oracle/), with the reference's FFT
+worker count min(8, cores), for a bounded number of steps; it imports nothing
+from palinstrophy_gb300.
+
+rel_l2_fp32_vs_oracle_100_steps: the FP64 oracle runs 100 steps from the same
+start in a spawned process while the GPU legs run; the FP32 form and the FP64
+plain path then replay its dt / cn sequence and are compared with it.
 """
 from __future__ import annotations
 
@@ -461,10 +467,13 @@ def _generator_times(N=N_GRID):
 
 
 def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
-    """FP32 CPU port of the reference path: steps/s over a bounded sample."""
+    """FP32 CPU port of the reference path (the oracle's FP32 mode, which is the
+    reference's NumPy/scipy.fft step operation for operation, with the reference's
+    elementwise passes on one thread as NumPy runs them): steps/s over a bounded
+    sample after one warm-up step."""
     import numpy as np
     from oracle import dns_oracle as do
-    S = do.OracleState(N_GRID, om2, uc, visc, CFL, dtype=np.float32, workers=workers)
+    S = do.OracleState(N_GRID, om2, uc, visc, CFL, dtype=np.float32, workers=workers, threads=1)
     do.init_dt(S)
     do.rk3(S)  # warm-up
     n, t0 = 0, time.perf_counter()
@@ -473,6 +482,80 @@ def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
         n += 1
     dt = time.perf_counter() - t0
     return n / dt, n, dt
+
+
+def _oracle_worker(N, om2, uc, visc, steps, out_dir):
+    """FP64 oracle run from the identical start (spawned process, no CUDA): the
+    final om2 and the NEXTDT log (it, t, dt, cn, cflm) into out_dir."""
+    import numpy as np
+    from oracle import dns_oracle as do
+    n = os.cpu_count() or 1
+    S = do.OracleState(N, om2, uc, visc, CFL, dtype=np.float64, workers=n, threads=n)
+    do.init_dt(S)
+    dt0 = S.dt
+    log = []
+    t0 = time.perf_counter()
+    do.run(S, steps, METHOD, UPDATE, log=log)
+    secs = time.perf_counter() - t0
+    np.save(os.path.join(out_dir, "om2.npy"), S.om2)
+    np.save(os.path.join(out_dir, "log.npy"), np.array([(dt0, 0, 0, 0, 0)] + log, dtype=np.float64))
+    with open(os.path.join(out_dir, "secs"), "w") as f:
+        f.write(f"{secs} {n}")
+
+
+class _OracleRun:
+    """The FP64 oracle (oracle/dns_oracle.py) for `steps` LS-IMEX-RK3 steps at
+    N=4096, in a spawned process while the GPU legs run."""
+
+    def __init__(self, om2, uc, visc, steps=100):
+        import multiprocessing as mp
+        import tempfile
+        self.steps = steps
+        self.dir = tempfile.mkdtemp(prefix="pal_oracle_")
+        self.proc = mp.get_context("spawn").Process(target=_oracle_worker,
+                                                    args=(om2.shape[0], om2, uc, visc, steps, self.dir))
+        self.proc.start()
+
+    def result(self, timeout=1800):
+        import numpy as np
+        self.proc.join(timeout)
+        if self.proc.exitcode != 0:
+            raise RuntimeError(f"oracle process failed (exit code {self.proc.exitcode})")
+        om2 = np.load(os.path.join(self.dir, "om2.npy"))
+        log = np.load(os.path.join(self.dir, "log.npy"))
+        with open(os.path.join(self.dir, "secs")) as f:
+            secs, threads = f.read().split()
+        for name in ("om2.npy", "log.npy", "secs"):
+            os.remove(os.path.join(self.dir, name))
+        os.rmdir(self.dir)
+        return om2, log, float(secs), int(threads)
+
+
+def _vs_oracle(om2, uc, visc, oracle):
+    """rel-L2 of om2 after the oracle's steps, FP32 form and FP64 plain path from
+    the identical start, the oracle's dt / cn sequence replayed into the GPU run."""
+    from palinstrophy_gb300.turbo_simulator import Field
+    o_om2, log, secs, threads = oracle.result()
+    dt0, marks = float(log[0, 0]), log[1:]
+    out = {}
+    for prec in ("fp32", "fp64"):
+        F = Field(N_GRID, prec, RE, CFL)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", visc)
+        F.step2a()
+        F.set_scalar("dt", dt0)
+        F.set_scalar("cn", 1.0)
+        F.set_scalar("cnm1", 0.0)
+        done = 0
+        for row in marks:
+            F.step(METHOD, int(row[0]) - done, update=0)
+            done = int(row[0])
+            F.set_scalar("dt", float(row[2]))
+            F.set_scalar("cn", float(row[3]))
+        out[prec] = _rel_l2(F.om2(), o_om2)
+        F.close()
+    return out["fp32"], out["fp64"], {"steps": oracle.steps, "oracle_s": secs, "oracle_threads": threads,
+                                      "dt_replayed": True, "oracle": "oracle/dns_oracle.py FP64 (numpy/scipy.fft)"}
 
 
 def _cpu_name():
@@ -487,21 +570,29 @@ def _cpu_name():
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host: the oracle's
+    FP32 port of the NumPy/scipy.fft step (pinned bit for bit to the reference's
+    own outputs by tests/test_oracle_golden.py; the Python reference itself is not
+    installed here), from the reference generator's N=4096 field restated in
+    oracle/pao_generator.py, with the reference's FFT worker count min(8, cores).
+    Nothing from palinstrophy_gb300 is imported on this path."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    om2, uc, st = _init_arrays()
-    workers = os.cpu_count() or 1
-    rate, n, secs = _cpu_port_rate(max(1, args.steps), 90.0, workers, om2, uc, st["visc"])
+    from oracle import pao_generator as pg
+    g = pg.generate_fast(N_GRID, K0, RE, SEED, "KM3")
+    workers = min(8, os.cpu_count() or 1)
+    rate, n, secs = _cpu_port_rate(max(1, args.steps), 120.0, workers, g["om2"], g["uc_low"], float(g["visc"]))
+    sample = (f"{n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up step ({secs:.1f} s), FP32 numpy/scipy.fft "
+              f"port of the reference path (oracle/dns_oracle.py), scipy.fft workers={workers} "
+              f"(the reference's min(8, cores)), {os.cpu_count()} host cores, {_cpu_name()}")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": n, "warmup": 1, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (KM3 generator, seed 4895)",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (reference KM3 generator restated, seed 4895)",
         "config": {"workload": WORKLOAD.replace("FP32 form (FP64 dt/CFL/diagnostic scalars)",
                                                 "reference FP32 CPU path (numpy + scipy.fft)"), "N": N_GRID},
-        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": workers, "kind": "port",
-                         "sample": f"{n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up step ({secs:.1f} s), "
-                                   f"scipy.fft workers={workers}, {_cpu_name()}"},
+        "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": workers, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -549,6 +640,7 @@ def run_gb300(args):
     B.close()
 
     e2e_rate, h2d, d2h = _e2e("fp32", om2, uc, visc, args.steps)
+    oracle = _OracleRun(om2, uc, visc, 100)
     ens = _ensemble_rate()
     diff = _differentiation()
     prec_form = _precision_form()
@@ -569,7 +661,9 @@ def run_gb300(args):
     dom_ms = max(ms_col, ms_row)
     dom_bytes = bytes_col if dominant == "k_col" else bytes_row
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
-    cpu_rate, cpu_n, cpu_s = _cpu_port_rate(3, 30.0, min(8, os.cpu_count() or 1), om2, uc, visc)
+    rel_oracle32, rel_oracle64, oracle_info = _vs_oracle(om2, uc, visc, oracle)
+    cpu_workers = min(8, os.cpu_count() or 1)
+    cpu_rate, cpu_n, cpu_s = _cpu_port_rate(20, 90.0, cpu_workers, om2, uc, visc)
     line = {
         "metric": METRIC,
         "value": rate32,
@@ -586,9 +680,13 @@ def run_gb300(args):
         "config": {"workload": WORKLOAD, "N": N_GRID, "M": 3 * N_GRID // 2, "method": METHOD,
                    "update": UPDATE, "l2": "state (0.67 GB FP32) larger than L2, no flush",
                    "parallelism": f"replicas x{ws}"},
-        "fp64": {"value": rate64, "unit": "steps/s", "steps": k64, "ms_per_step": ms64 / k64},
-        "fp32_over_fp64": rate32 / rate64,
-        "rel_l2_fp32_vs_fp64_100_steps": rel,
+        # the large nested blocks first, so that the headline keys close the line
+        "ensemble": ens,
+        "differentiation": diff,
+        "precision_form": prec_form,
+        "large_single_field": large,
+        "initial_condition": gen_times,
+        "oracle_check": oracle_info,
         "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         # timed region = one pal_step call: 6 launches per RK3 step, the two om/fnm1
         # order conversions, and a k_phys launch if the last step ends on the NEXTDT cadence
@@ -599,16 +697,17 @@ def run_gb300(args):
                      "ms_per_launch": {"k_row": ms_row, "k_col": ms_col},
                      "limiter": _limiter(dominant, "fp32"),
                      "stage_bytes_per_s": (bytes_row + bytes_col) / ((ms_row + ms_col) / 1000.0) / 1e9},
-        "ensemble": ens,
-        "differentiation": diff,
-        "precision_form": prec_form,
-        "large_single_field": large,
-        "initial_condition": gen_times,
-        "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": min(8, os.cpu_count() or 1),
+        "cpu_baseline": {"value": cpu_rate, "unit": "steps/s", "cores": cpu_workers,
                          "kind": "port",
                          "sample": f"{cpu_n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up ({cpu_s:.1f} s), FP32 "
-                                   f"numpy/scipy.fft port of the reference path, {_cpu_name()}"},
+                                   f"numpy/scipy.fft port of the reference path, scipy.fft workers={cpu_workers} "
+                                   f"(the reference's min(8, cores)), {_cpu_name()}"},
         "clocks": clocks,
+        "fp64": {"value": rate64, "unit": "steps/s", "steps": k64, "ms_per_step": ms64 / k64},
+        "fp32_over_fp64": rate32 / rate64,
+        "rel_l2_fp32_vs_fp64_100_steps": rel,
+        "rel_l2_fp64_vs_oracle_100_steps": rel_oracle64,
+        "rel_l2_fp32_vs_oracle_100_steps": rel_oracle32,
     }
     print(json.dumps(line), flush=True)
 

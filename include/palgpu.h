@@ -236,9 +236,25 @@ int pal_generate(pal_handle* h, double K0, double Re, int seed, int spectrum, vo
 
 /* Host-side PAO / KM3 initial condition (turbo_simulator.py:213-485, 1059-1239,
  * 1314-1361), complex64 outputs: om2 (N, N/2) and uc_low (2, N, N/2).
- * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed. */
+ * stats[0..2] = Energy (Q2), WiWi (W2), visc; *seed_out = final LCG seed.
+ * The per-mode float32 cos/sin/exp come from the C library here; the reference
+ * takes them from NumPy's float32 ufuncs, which can differ in the last bit. */
 int pal_pao_generate(int N, double K0, double Re, int seed, int spectrum, void* om2, void* uc_low,
                      double* stats, int* seed_out);
+/* The generator in two halves around its three float32 transcendental values,
+ * so that a caller can evaluate those with the reference's own functions
+ * (NumPy's float32 ufuncs) and reproduce the reference's arrays bit for bit.
+ * pal_pao_draws: the serial LCG + 97-entry shuffle of turbo_simulator.py:241-286;
+ * v[z * N/2 + x] = the shuffled variate of mode (x, z) in the reference's call
+ * order, *seed_out = final LCG seed.
+ * pal_pao_build: turbo_simulator.py:287-470 and 1314-1361 from
+ * cos_th = cos(2 pi v), sin_th = sin(2 pi v) (2 pi v formed as
+ * (float(2) * float(pi)) * v) and exp_g = exp(-(k/K0)^2) (k = sqrt(float(kx^2 +
+ * kz^2)), -(k/K0) * (k/K0) in float), all float32 in the layout of v; outputs as
+ * pal_pao_generate. */
+int pal_pao_draws(int N, int seed, float* v, int* seed_out);
+int pal_pao_build(int N, double K0, double Re, int seed, int spectrum, const float* cos_th, const float* sin_th,
+                  const float* exp_g, void* om2, void* uc_low, double* stats);
 
 #ifdef __cplusplus
 }

@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import math
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import scipy.fft as spfft
@@ -38,10 +39,31 @@ RK3_ALPHA = (8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0)
 RK3_BETA = (0.0, -17.0 / 60.0, -5.0 / 12.0)
 
 
+_POOL = {}
+
+
+def _rows(S, n, fn):
+    """Run fn(slice) over blocks of rows 0..n-1 on S.threads host threads.
+
+    Only elementwise work goes through here: each output element is computed by
+    the same NumPy operations whatever the split, so the results are identical
+    to one call over all rows (NumPy releases the GIL inside large ufunc calls).
+    """
+    k = S.threads
+    if k <= 1 or n < 64 * k:
+        fn(slice(0, n))
+        return
+    pool = _POOL.get(k)
+    if pool is None:
+        pool = _POOL[k] = ThreadPoolExecutor(k)
+    b = -(-n // k)
+    list(pool.map(fn, [slice(i, min(n, i + b)) for i in range(0, n, b)]))
+
+
 class OracleState:
     """Minimal DnsState twin holding the arrays and scalars one step touches."""
 
-    def __init__(self, N, om2, uc_low, visc, cflnum, dtype=np.float64, workers=None):
+    def __init__(self, N, om2, uc_low, visc, cflnum, dtype=np.float64, workers=None, threads=None):
         if N % 4:
             raise ValueError("N must be a multiple of 4")
         self.rdt = np.dtype(dtype)
@@ -55,6 +77,8 @@ class OracleState:
         # passes min(8, cpu_count) (turbo_simulator.py:912), so the FP32 port
         # is bit-exact with it only at that same count.
         self.workers = workers if workers else min(8, os.cpu_count() or 1)
+        # host threads for the elementwise passes (results do not depend on it)
+        self.threads = threads if threads else (os.cpu_count() or 1)
         M, Nh = self.M, self.Nh
         self.ur_full = np.zeros((3, M, M), self.rdt)
         self.uc_full = np.zeros((3, M, self.NK_full), self.cdt)
@@ -97,35 +121,62 @@ def step2a(S: OracleState) -> None:
     N, Nh = S.N, S.Nh
     UC = S.uc_full
     hi_end = min(3 * N // 4, S.NK_full - 1)
-    UC[0:2, :, Nh:hi_end + 1] = 0
-    UC[0:2, N:N + Nh, :Nh] = UC[0:2, Nh:N, :Nh]
-    UC[0:2, Nh:N, :Nh] = 0
+
+    def pad(sl):
+        UC[0:2, sl, Nh:hi_end + 1] = 0
+
+    def move(sl):  # rows Nh..N-1 -> N..N+Nh-1 (disjoint ranges), then zero the source
+        src = slice(Nh + sl.start, Nh + sl.stop)
+        UC[0:2, N + sl.start:N + sl.stop, :Nh] = UC[0:2, src, :Nh]
+        UC[0:2, src, :Nh] = 0
+
+    _rows(S, S.M, pad)
+    _rows(S, Nh, move)
     ur01 = spfft.irfft2(UC[0:2], axes=(1, 2), overwrite_x=True,
                         workers=S.workers, norm="forward")
-    S.ur_full[0:2] = ur01
+
+    def put(sl):
+        S.ur_full[0:2, sl] = ur01[:, sl]
+
+    _rows(S, S.M, put)
 
 
 def step2b(S: OracleState) -> None:
     """In-place products, forward rfft2 of the 3 planes, zero row z=N (TS:1449-1513)."""
     UR = S.ur_full
-    u, w = UR[0], UR[1]
-    np.multiply(u, w, out=UR[2])
-    np.multiply(u, u, out=UR[0])
-    np.multiply(w, w, out=UR[1])
-    S.uc_full[...] = spfft.rfft2(UR, axes=(1, 2), overwrite_x=True, workers=S.workers)
+
+    def products(sl):
+        u, w = UR[0, sl], UR[1, sl]
+        np.multiply(u, w, out=UR[2, sl])
+        np.multiply(u, u, out=u)
+        np.multiply(w, w, out=w)
+
+    _rows(S, S.M, products)
+    S.uc_full = spfft.rfft2(UR, axes=(1, 2), overwrite_x=True, workers=S.workers)
     S.uc_full[0:3, S.N, 0:S.Nh] = 0
 
 
 def nonlinear(S: OracleState) -> np.ndarray:
-    """fn = divxz [GA (F uu - F ww) + (G^2 - A^2) F uw] at gathered rows (TS:1520-1552)."""
+    """fn = divxz [GA (F uu - F ww) + (G^2 - A^2) F uw] at gathered rows (TS:1520-1552).
+
+    Output row z < N/2 reads uc_full row z, row z >= N/2 reads row z + N/2."""
     N, Nh = S.N, S.Nh
-    low = S.uc_full[:, :, :Nh]
-    g = np.concatenate([low[:, :Nh], low[:, N:N + Nh]], axis=1)  # (3, N, Nh)
-    out = np.subtract(g[0], g[1])
-    np.multiply(out, S.GA, out=out)
-    tmp = np.multiply(g[2], S.G2mA2)
-    np.add(out, tmp, out=out)
-    np.multiply(out, S.divxz, out=out)
+    UC = S.uc_full
+    out = np.empty((N, Nh), S.cdt)
+
+    def blk(sl):
+        for lo, hi, off in ((sl.start, min(sl.stop, Nh), 0), (max(sl.start, Nh), sl.stop, Nh)):
+            if lo >= hi:
+                continue
+            o, g = slice(lo, hi), slice(lo + off, hi + off)
+            r = np.subtract(UC[0, g, :Nh], UC[1, g, :Nh])
+            np.multiply(r, S.GA[o], out=r)
+            tmp = np.multiply(UC[2, g, :Nh], S.G2mA2[o])
+            np.add(r, tmp, out=r)
+            np.multiply(r, S.divxz, out=r)
+            out[o] = r
+
+    _rows(S, N, blk)
     return out
 
 
@@ -133,21 +184,27 @@ def reconstruct_velocity(S: OracleState) -> None:
     """omega -> (u1, u3) low band of uc_full (TS:1555-1585)."""
     N, Nh = S.N, S.Nh
     om = S.om2
-    out1 = np.zeros_like(om)
-    out2 = np.zeros_like(om)
+    UC = S.uc_full
     mi = S.cdt.type(-1j)
     pi_ = S.cdt.type(1j)
-    if Nh > 1:
-        o1 = om[:, 1:] * S.invK2_sub
-        o1 = o1 * S.gamma[:, None]
-        out1[:, 1:] = o1 * mi
-        o2 = om[:, 1:] * S.invK2_sub
-        o2 = o2 * S.alfa[1:][None, :]
-        out2[:, 1:] = o2 * pi_
-    out1[:, 0] = mi * om[:, 0] * S.inv_gamma0
-    out2[:, 0] = 0
-    S.uc_full[0, :N, :Nh] = out1
-    S.uc_full[1, :N, :Nh] = out2
+
+    def blk(sl):
+        o = om[sl]
+        out1 = np.zeros_like(o)
+        out2 = np.zeros_like(o)
+        if Nh > 1:
+            o1 = o[:, 1:] * S.invK2_sub[sl]
+            o1 = o1 * S.gamma[sl, None]
+            out1[:, 1:] = o1 * mi
+            o2 = o[:, 1:] * S.invK2_sub[sl]
+            o2 = o2 * S.alfa[1:][None, :]
+            out2[:, 1:] = o2 * pi_
+        out1[:, 0] = mi * o[:, 0] * S.inv_gamma0[sl]
+        out2[:, 0] = 0
+        UC[0, sl, :Nh] = out1
+        UC[1, sl, :Nh] = out2
+
+    _rows(S, N, blk)
 
 
 def step3(S: OracleState) -> None:
@@ -156,14 +213,21 @@ def step3(S: OracleState) -> None:
     visc, dt, cnm1 = s(S.visc), s(S.dt), s(S.cnm1)
     fn = nonlinear(S)
     vt = s(0.5) * visc * dt
-    arg = S.K2 * vt
-    den = arg + s(1.0)
     c2 = s(0.5) * dt * (s(2.0) + cnm1)
     c3 = -s(0.5) * dt * cnm1
-    num = S.om2 - S.om2 * arg
-    num = num + fn * c2
-    num = num + S.fnm1 * c3
-    S.om2 = (num / den).astype(S.cdt)
+    om, fm = S.om2, S.fnm1
+    new = np.empty_like(om)
+
+    def blk(sl):
+        arg = S.K2[sl] * vt
+        den = arg + s(1.0)
+        num = om[sl] - om[sl] * arg
+        num = num + fn[sl] * c2
+        num = num + fm[sl] * c3
+        new[sl] = num / den
+
+    _rows(S, S.N, blk)
+    S.om2 = new
     S.fnm1 = fn
     reconstruct_velocity(S)
     S.cnm1 = float(S.cn)
@@ -177,12 +241,20 @@ def rk3(S: OracleState) -> None:
         a, b = s(a_), s(b_)
         step2b(S)
         fn = nonlinear(S)
-        rhs = s(1.0) - S.K2 * (b * dt * visc)
-        num = S.om2 * rhs
-        num = num + fn * (a * dt)
-        num = num + S.fnm1 * (b * dt)
-        den = S.K2 * (a * dt * visc) + s(1.0)
-        S.om2 = (num / den).astype(S.cdt)
+        kb, fa, fb, ka = b * dt * visc, a * dt, b * dt, a * dt * visc
+        om, fm = S.om2, S.fnm1
+        new = np.empty_like(om)
+
+        def blk(sl):
+            rhs = s(1.0) - S.K2[sl] * kb
+            num = om[sl] * rhs
+            num = num + fn[sl] * fa
+            num = num + fm[sl] * fb
+            den = S.K2[sl] * ka + s(1.0)
+            new[sl] = num / den
+
+        _rows(S, S.N, blk)
+        S.om2 = new
         S.fnm1 = fn
         reconstruct_velocity(S)
         step2a(S)

@@ -94,6 +94,8 @@ _SIGS = {
     "pal_ensemble_last_error": (_I, [_H, ctypes.c_char_p, ctypes.c_size_t]),
     "pal_step_noalloc": (_I, [_I, _I, _I, _D, _D, _D, _D, _P, _P, _P]),
     "pal_pao_generate": (_I, [_I, _D, _D, _I, _I, _P, _P, _DP, ctypes.POINTER(_I)]),
+    "pal_pao_draws": (_I, [_I, _I, _P, ctypes.POINTER(_I)]),
+    "pal_pao_build": (_I, [_I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _DP]),
 }
 
 _lib = None
@@ -148,7 +150,48 @@ def ptr(a: np.ndarray):
 
 
 def pao_generate(N, K0, Re, seed, spectrum="KM3"):
-    """Host generator: returns (om2 (N,N/2) c64, uc_low (2,N,N/2) c64, stats dict)."""
+    """Host generator: returns (om2 (N,N/2) c64, uc_low (2,N,N/2) c64, stats dict).
+
+    The reference's own field, bit for bit on the machine it runs on: the serial
+    LCG draws (pal_pao_draws) and everything after the three per-mode float32
+    transcendental values (pal_pao_build) run in C++; those three values --
+    cos and sin of the phase 2 pi v and exp(-(k/K0)^2) -- are NumPy's float32
+    ufuncs, as the reference evaluates them (turbo_simulator.py:287-318).
+    """
+    N = int(N)
+    if N < 8 or N % 4:
+        raise ValueError("N must be a multiple of 4 and >= 8")
+    spec = {"KM3": PAL_SPEC_KM3, "PAO": PAL_SPEC_PAO}[spectrum.upper()]
+    lib = load()
+    nh = N // 2
+    v = np.empty((N, nh), np.float32)
+    so = ctypes.c_int(0)
+    check(lib.pal_pao_draws(N, int(seed), ptr(v), ctypes.byref(so)))
+    pi = np.float32(3.14159265358979)
+    th = (np.float32(2.0) * pi) * v
+    cos_th = np.cos(th)
+    sin_th = np.sin(th)
+    alfa = np.arange(nh, dtype=np.float32)
+    z = np.arange(N)
+    gamma = np.where(z < nh, z, z - N).astype(np.float32)
+    k2 = (gamma * gamma)[:, None] + (alfa * alfa)[None, :]
+    k = np.sqrt(k2)
+    t = k / np.float32(K0)
+    exp_g = np.exp((-t) * t)
+    om2 = np.zeros((N, nh), np.complex64)
+    uc = np.zeros((2, N, nh), np.complex64)
+    st = (ctypes.c_double * 3)()
+    check(lib.pal_pao_build(N, float(K0), float(Re), int(seed), spec, ptr(cos_th), ptr(sin_th), ptr(exp_g),
+                            ptr(om2), ptr(uc), st))
+    # om2 = i (gamma u1 - alfa u3) with NumPy's complex64 arithmetic, so that even
+    # the signs of zero modes are the reference's (turbo_simulator.py:1314-1361)
+    d = gamma[:, None] * uc[0] - alfa[None, :] * uc[1]
+    om2 = np.asarray(-d.imag + 1j * d.real, dtype=np.complex64)
+    return om2, uc, {"Energy": st[0], "WiWi": st[1], "visc": st[2], "seed_out": so.value}
+
+
+def pao_generate_libm(N, K0, Re, seed, spectrum="KM3"):
+    """The same generator with the C library's float32 cos/sin/exp (pal_pao_generate)."""
     spec = {"KM3": PAL_SPEC_KM3, "PAO": PAL_SPEC_PAO}[spectrum.upper()]
     om2 = np.zeros((N, N // 2), np.complex64)
     uc = np.zeros((2, N, N // 2), np.complex64)

@@ -9,9 +9,15 @@
 //   om2 = i (gamma u1 - alfa u3) (dnsCudaCalcom) .... 1314-1361
 // The reference evaluates the PAO part with NumPy float32 scalars; it is kept
 // in float here (compile with -ffp-contract=off so no multiply-add is fused).
-// The float32 exp/sin/cos come from the C library, which can differ from
-// NumPy's vectorised float32 kernels in the last bit; the KM3 part is double
-// precision and reproduces the reference bit for bit.
+// Its three float32 transcendental values per mode -- cos and sin of the
+// random phase 2 pi v and exp(-(k/K0)^2) -- are NumPy's own ufuncs in the
+// reference, which the C library's cosf/sinf/expf can miss by an ulp.  So the
+// generator is split: pal_pao_draws runs the serial LCG, the caller evaluates
+// the three values (palinstrophy_gb300/_lib.py does it with NumPy's float32
+// ufuncs, which gives the reference's field bit for bit), and pal_pao_build
+// does everything else.  pal_pao_generate is the same pipeline with the C
+// library's functions, for C callers.  The KM3 part is double precision with
+// the C library's sin/cos/sqrt, as Python's math module uses them.
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -33,29 +39,30 @@ double hash01(int x, int z, int seed, int salt) {
   return s - std::floor(s);
 }
 
-// complex64(real a) * (c + i s) as NumPy evaluates it
-inline cf scale(float a, cf p) { return cf(a * p.real(), a * p.imag()); }
+// complex64(a) * p as NumPy multiplies two complex64 scalars: (a + 0i)(pr + i pi)
+inline cf scale(float a, cf p) {
+  const float zero = 0.0f;
+  return cf(a * p.real() - zero * p.imag(), a * p.imag() + zero * p.real());
+}
 
-}  // namespace
-
-extern "C" int pal_pao_generate(int N, double K0d, double Re, int seed_init, int spectrum, void* om2_out,
-                                void* uc_out, double* stats, int* seed_out) {
-  if (N < 8 || N % 4 != 0 || !om2_out || !uc_out) return PAL_ERR_INVALID;
-  if (spectrum != PAL_SPEC_KM3 && spectrum != PAL_SPEC_PAO) return PAL_ERR_INVALID;
-  const bool km3 = spectrum == PAL_SPEC_KM3;
+void wavenumbers(int N, std::vector<float>& alfa, std::vector<float>& gamma) {
   const int nh = N / 2;
-  const float PI = 3.14159265358979f;
-  const float K0 = (float)K0d;
-  std::vector<float> alfa(nh), gamma(N, 0.0f);
+  alfa.assign(nh, 0.0f);
+  gamma.assign(N, 0.0f);
   for (int x = 0; x < nh; ++x) alfa[x] = (float)x;
   for (int z = 1; z <= nh; ++z) {
     gamma[z] = (float)z;
     gamma[N - z] = -gamma[z];
   }
-  // ur[(x * N + z) * 2 + c]
-  std::vector<cf> ur((size_t)nh * N * 2, cf(0.0f, 0.0f));
-  auto U = [&](int x, int z, int c) -> cf& { return ur[((size_t)x * N + z) * 2 + c]; };
+}
 
+}  // namespace
+
+// Serial LCG draws of the PAO loop (turbo_simulator.py:241-286): v[z * N/2 + x]
+// is the shuffled uniform variate of mode (x, z), in the reference's call order.
+extern "C" int pal_pao_draws(int N, int seed_init, float* v, int* seed_out) {
+  if (N < 8 || N % 4 != 0 || !v) return PAL_ERR_INVALID;
+  const int nh = N / 2;
   int64_t s = seed_init;
   for (int i = 0; i < 97; ++i) s = (s * kImm + kIt) % kId;
   float table[97];
@@ -63,32 +70,54 @@ extern "C" int pal_pao_generate(int N, double K0d, double Re, int seed_init, int
     s = (s * kImm + kIt) % kId;
     table[i] = (float)s / (float)kId;
   }
-  const float norm = (PI * K0) * K0;
-  const float floor2 = 1.0e-40f;
   for (int z = 0; z < N; ++z) {
-    const float gz = gamma[z];
     for (int x = 0; x < nh; ++x) {
       s = (s * kImm + kIt) % kId;
       const float r = (float)s / (float)kId;
       int idx = (int)((double)r * 97.0);
       idx = idx < 0 ? 0 : (idx > 96 ? 96 : idx);
-      const float v = table[idx];
+      v[(size_t)z * nh + x] = table[idx];
       table[idx] = r;
-      const float th = (2.0f * PI) * v;
-      const cf phase(std::cos(th), std::sin(th));
+    }
+  }
+  if (seed_out) *seed_out = (int)s;
+  return PAL_OK;
+}
+
+// Everything after the draws (turbo_simulator.py:287-470, 1314-1361), given the
+// per-mode float32 values cos_th = cos(2 pi v), sin_th = sin(2 pi v) and
+// exp_g = exp(-(k/K0)^2) in the layout of pal_pao_draws.
+extern "C" int pal_pao_build(int N, double K0d, double Re, int seed_init, int spectrum, const float* cos_th,
+                             const float* sin_th, const float* exp_g, void* om2_out, void* uc_out,
+                             double* stats) {
+  if (N < 8 || N % 4 != 0 || !om2_out || !uc_out || !cos_th || !sin_th || !exp_g) return PAL_ERR_INVALID;
+  if (spectrum != PAL_SPEC_KM3 && spectrum != PAL_SPEC_PAO) return PAL_ERR_INVALID;
+  const bool km3 = spectrum == PAL_SPEC_KM3;
+  const int nh = N / 2;
+  const float PI = 3.14159265358979f;
+  const float K0 = (float)K0d;
+  std::vector<float> alfa, gamma;
+  wavenumbers(N, alfa, gamma);
+  // ur[(x * N + z) * 2 + c]
+  std::vector<cf> ur((size_t)nh * N * 2, cf(0.0f, 0.0f));
+  auto U = [&](int x, int z, int c) -> cf& { return ur[((size_t)x * N + z) * 2 + c]; };
+
+  const float norm = (PI * K0) * K0;
+  const float floor2 = 1.0e-40f;
+  for (int z = 0; z < N; ++z) {
+    const float gz = gamma[z];
+    for (int x = 0; x < nh; ++x) {
+      const size_t m = (size_t)z * nh + x;
+      const cf phase(cos_th[m], sin_th[m]);
       const float ax = alfa[x];
-      const float k2 = ax * ax + gz * gz;
-      const float k = k2 > 0.0f ? std::sqrt(k2) : 0.0f;
-      const float t = k / K0;
-      const float g = -t * t;
       if (ax == 0.0f) {
-        float e2 = std::exp(g) / norm;
+        float e2 = exp_g[m] / norm;
         if (km3 && e2 < floor2) e2 = floor2;
         U(x, z, 1) = cf(0.0f, 0.0f);
         U(x, z, 0) = scale(std::sqrt(e2), phase);
       } else {
         const float den = 1.0f + (gz * gz) / (ax * ax);
-        float e2 = std::exp(g) / (den * norm);
+        float e2 = exp_g[m] / (den * norm);
         if (km3 && e2 < floor2) e2 = floor2;
         const cf w = scale(std::sqrt(e2), phase);
         U(x, z, 1) = w;
@@ -198,7 +227,6 @@ extern "C" int pal_pao_generate(int N, double K0d, double Re, int seed_init, int
     stats[1] = a3 + a4 + a5 + a6;
     stats[2] = (double)visc;
   }
-  if (seed_out) *seed_out = (int)s;
 
   // outputs: uc_low (2, N, nh) [c][z][x]; om2 (N, nh) = i (gz u1 - ax u3)
   cf* uc = static_cast<cf*>(uc_out);
@@ -215,4 +243,31 @@ extern "C" int pal_pao_generate(int N, double K0d, double Re, int seed_init, int
     }
   }
   return PAL_OK;
+}
+
+extern "C" int pal_pao_generate(int N, double K0d, double Re, int seed_init, int spectrum, void* om2_out,
+                                void* uc_out, double* stats, int* seed_out) {
+  if (N < 8 || N % 4 != 0 || !om2_out || !uc_out) return PAL_ERR_INVALID;
+  if (spectrum != PAL_SPEC_KM3 && spectrum != PAL_SPEC_PAO) return PAL_ERR_INVALID;
+  const int nh = N / 2;
+  const size_t n = (size_t)N * nh;
+  std::vector<float> v(n), c(n), sn(n), e(n), alfa, gamma;
+  int rc = pal_pao_draws(N, seed_init, v.data(), seed_out);
+  if (rc != PAL_OK) return rc;
+  wavenumbers(N, alfa, gamma);
+  const float PI = 3.14159265358979f;
+  const float K0 = (float)K0d;
+  for (int z = 0; z < N; ++z) {
+    for (int x = 0; x < nh; ++x) {
+      const size_t m = (size_t)z * nh + x;
+      const float th = (2.0f * PI) * v[m];
+      c[m] = std::cos(th);
+      sn[m] = std::sin(th);
+      const float k2 = alfa[x] * alfa[x] + gamma[z] * gamma[z];
+      const float k = k2 > 0.0f ? std::sqrt(k2) : 0.0f;
+      const float t = k / K0;
+      e[m] = std::exp(-t * t);
+    }
+  }
+  return pal_pao_build(N, K0d, Re, seed_init, spectrum, c.data(), sn.data(), e.data(), om2_out, uc_out, stats);
 }

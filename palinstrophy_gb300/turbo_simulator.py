@@ -17,8 +17,10 @@ The names, signatures and DnsState fields mirror
   run_dns / compare_time_steppers turbo_simulator.py:2744-2903
 
 Every step runs in the hand-written sm_103a kernels of libpalgpu.so; there is
-no CPU path here.  Array fields (om2, fnm1, ur_full, ...) are host NumPy copies
-taken on access, as the reference GUI does with cp.asnumpy at frame pulls.
+no CPU path here.  om2 and fnm1 are host NumPy copies taken on access, as the
+reference GUI does with cp.asnumpy at frame pulls; ur_full is a persistent host
+array whose velocity planes refresh from the device when read after a step and
+whose third plane holds the display helpers' output, as in the reference.
 """
 from __future__ import annotations
 
@@ -71,6 +73,8 @@ class Field:
         h = L._H()
         L.check(self.lib.pal_create(self.N, _PREC[precision], float(Re), float(cfl), h))
         self.h = h
+        # bumped by every call that changes the field, so host copies know when they are stale
+        self.gen = 0
 
     # -- lifetime ---------------------------------------------------------
     def close(self):
@@ -89,6 +93,7 @@ class Field:
 
     # -- state ------------------------------------------------------------
     def set_state(self, om2, fnm1=None, uc_low=None):
+        self.gen += 1
         om2 = np.ascontiguousarray(om2, dtype=self.cdt)
         if om2.shape != (self.N, self.N // 2):
             raise ValueError(f"om2 must have shape {(self.N, self.N // 2)}")
@@ -103,6 +108,7 @@ class Field:
     def generate(self, K0: float, Re: float, seed: int, spectrum: str = "KM3"):
         """PAO / KM3 start generated on the device (pal_generate); returns
         (uc_low (2, N, N/2) host copy, stats dict as pao_generate's)."""
+        self.gen += 1
         spec = {"KM3": L.PAL_SPEC_KM3, "PAO": L.PAL_SPEC_PAO}[spectrum.upper()]
         uc = np.empty((2, self.N, self.N // 2), self.cdt)
         st = (L._D * 3)()
@@ -127,18 +133,23 @@ class Field:
 
     # -- stepping -----------------------------------------------------------
     def step2a(self):
+        self.gen += 1
         self._ck(self.lib.pal_step2a(self.h))
 
     def step2b(self):
+        self.gen += 1
         self._ck(self.lib.pal_step2b(self.h))
 
     def step3(self):
+        self.gen += 1
         self._ck(self.lib.pal_step3(self.h))
 
     def step_rk3(self):
+        self.gen += 1
         self._ck(self.lib.pal_step_rk3(self.h))
 
     def step(self, method="CNAB2", nsteps=1, update=0, final_update=False):
+        self.gen += 1
         self._ck(self.lib.pal_step(self.h, _METHODS[method], int(nsteps), int(update), int(bool(final_update))))
 
     def compute_cflm(self) -> float:
@@ -202,20 +213,31 @@ class Field:
 
     def ur(self, comp: int):
         a = np.empty((self.M, self.M), self.rdt)
-        self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_UR_U if comp == 0 else L.PAL_FIELD_UR_V, L.ptr(a)))
-        return a
+        return self.ur_into(comp, a)
+
+    def ur_into(self, comp: int, out):
+        """Physical u (comp 0) or v (1) into a C-contiguous (M, M) host array."""
+        if out.shape != (self.M, self.M) or out.dtype != self.rdt or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous ({self.M}, {self.M}) {np.dtype(self.rdt).name} array")
+        self._ck(self.lib.pal_get_field(self.h, L.PAL_FIELD_UR_U if comp == 0 else L.PAL_FIELD_UR_V, L.ptr(out)))
+        return out
 
     def adjoint_palinstrophy(self, nsteps: int, ckpt_every: int = 20):
         """(L, dL/d om2) for L = final palinstrophy after nsteps fixed-dt RK3 steps."""
+        self.gen += 1
         g = np.empty((self.N, self.N // 2), self.cdt)
         loss = L._D()
         self._ck(self.lib.pal_adjoint_palinstrophy(self.h, int(nsteps), int(ckpt_every), L.ctypes.byref(loss),
                                                    L.ptr(g)))
         return loss.value, g
 
-    def vis(self, var: int, field: bool = True, pixels: bool = False):
-        """Display field var (VAR_U..VAR_STREAM): (float field or None, uint8 pixels or None)."""
-        f = np.empty((self.M, self.M), self.rdt) if field else None
+    def vis(self, var: int, field: bool = True, pixels: bool = False, out=None):
+        """Display field var (VAR_U..VAR_STREAM): (float field or None, uint8 pixels or None);
+        `out`, a C-contiguous (M, M) array of the handle's real type, receives the field."""
+        if out is not None and (out.shape != (self.M, self.M) or out.dtype != self.rdt
+                                or not out.flags.c_contiguous):
+            raise ValueError(f"out must be a C-contiguous ({self.M}, {self.M}) {np.dtype(self.rdt).name} array")
+        f = out if out is not None else (np.empty((self.M, self.M), self.rdt) if field else None)
         p = np.empty((self.M, self.M), np.uint8) if pixels else None
         self._ck(self.lib.pal_vis_field(self.h, int(var), None if f is None else L.ptr(f),
                                         None if p is None else p.ctypes.data_as(L.ctypes.POINTER(L.ctypes.c_ubyte))))
@@ -262,6 +284,61 @@ class _DeviceView:
                                          "strides": tuple(strides), "version": 3, "stream": None}
 
 
+class _UrFull:
+    """`DnsState.ur_full`, the (3, M, M) physical planes of the reference state.
+
+    A persistent host array: plane 0 (u) and plane 1 (v) are copied from the
+    device when read after the field changed (per plane, so reading one plane
+    moves one plane), and plane 2 keeps what the display helpers -- or the
+    caller -- last wrote into it, as the reference's dns_kinetic, dns_om2_phys
+    and dns_stream_func leave their result in ur_full[2]
+    (turbo_simulator.py:2629-2711) for DnsSimulator.make_pixels_component to
+    read (turbo_wrapper.py:436-470).  Indexing returns views of the persistent
+    array, refreshed in place; host writes into planes 0 and 1 are not sent to
+    the device and last until the field next changes.
+    """
+
+    def __init__(self, field):
+        self._f = field
+        self._a = np.zeros((3, field.M, field.M), field.rdt)
+        self._gen = [-1, -1]
+        self.shape, self.dtype, self.ndim, self.size = self._a.shape, self._a.dtype, 3, self._a.size
+
+    def _planes(self, key):
+        k = key[0] if isinstance(key, tuple) and key else key
+        if isinstance(k, (int, np.integer)):
+            return [int(k) % 3]
+        if isinstance(k, slice):
+            return list(range(3))[k]
+        return [0, 1, 2]
+
+    def _refresh(self, planes):
+        g = self._f.gen
+        for p in planes:
+            if p < 2 and self._gen[p] != g:
+                self._f.ur_into(p, self._a[p])
+                self._gen[p] = g
+
+    def plane2(self):
+        """The persistent plane 2 (the display helpers' output buffer)."""
+        return self._a[2]
+
+    def __getitem__(self, key):
+        self._refresh(self._planes(key))
+        return self._a[key]
+
+    def __setitem__(self, key, value):
+        self._refresh(self._planes(key))
+        self._a[key] = value
+
+    def __array__(self, dtype=None, copy=None):
+        self._refresh([0, 1])
+        return self._a if dtype is None else self._a.astype(dtype)
+
+    def __len__(self):
+        return 3
+
+
 class DnsState:
     """GB300 twin of the reference DnsState (turbo_simulator.py:654-810).
 
@@ -299,6 +376,7 @@ class DnsState:
         self.step3_K2 = (self.alfa[None, :] ** 2 + self.gamma[:, None] ** 2).astype(np.float32)
         f = Field(N, precision, Re, CFL)
         object.__setattr__(self, "_field", f)
+        object.__setattr__(self, "_ur", _UrFull(f))
         object.__setattr__(self, "visc", float(np.float32(1.0 / float(np.float32(Re)))))
         object.__setattr__(self, "cflnum", float(CFL))
         object.__setattr__(self, "dt", 0.0)
@@ -338,11 +416,8 @@ class DnsState:
 
     @property
     def ur_full(self):
-        u = self._field.ur(0)
-        out = np.zeros((3, self.NZ_full, self.NX_full), u.dtype)
-        out[0] = u
-        out[1] = self._field.ur(1)
-        return out
+        """(3, M, M): u, v and the display plane (see _UrFull)."""
+        return self._ur
 
     @property
     def ur(self):
@@ -378,10 +453,14 @@ class DnsState:
 def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float = 0.75,
                      backend: str = "gb300", seed: int = 1, skip_pao: bool = False,
                      populate_compact_ur: bool = True, start_spectrum: SPECTRUM = "KM3",
-                     precision: str = "fp32", generator: str = "device") -> DnsState:
-    """Allocate the GB300 state and run the PAO/KM3 generator (turbo_simulator.py:878-1054):
-    on the device (`generator="device"`, pal_generate) or with the host restatement
-    (`"host"`, pal_pao_generate)."""
+                     precision: str = "fp32", generator: str = "host") -> DnsState:
+    """Allocate the GB300 state and run the PAO/KM3 generator (turbo_simulator.py:878-1054).
+
+    `generator="host"` (default): the reference's own initial field bit for bit
+    (C++ LCG and shell sums, NumPy float32 cos/sin/exp as the reference evaluates
+    them; `_lib.pao_generate`), then uploaded.  `"device"`: pal_generate, the
+    per-mode work on the GPU (N=4096 in ~0.04 s), whose CUDA float32 functions
+    differ from NumPy's by a few ulp (<= 4e-7 relative)."""
     if backend not in ("gb300", "gpu", "auto"):
         raise ValueError(f"backend {backend!r}: this module is the GB300 backend (no CPU path)")
     S = DnsState(N, Re, K0, CFL, seed, start_spectrum, precision, populate_compact_ur)
@@ -410,19 +489,19 @@ def create_dns_state(N: int = 8, Re: float = 1e5, K0: float = 100.0, CFL: float 
 VAR_U, VAR_V, VAR_ENERGY, VAR_OMEGA, VAR_STREAM = 0, 1, 2, 3, 4
 
 
-def dns_kinetic(S: DnsState):
-    """|u| on the 3/2 grid (turbo_simulator.py:2629-2636); returned, not stored in ur_full[2]."""
-    return S.field.vis(VAR_ENERGY)[0]
+def dns_kinetic(S: DnsState) -> None:
+    """|u| = sqrt(u^2 + v^2) on the 3/2 grid into ur_full[2] (turbo_simulator.py:2629-2636)."""
+    S.field.vis(VAR_ENERGY, out=S.ur_full.plane2())
 
 
-def dns_om2_phys(S: DnsState):
-    """Physical vorticity from om2 (turbo_simulator.py:2684-2687)."""
-    return S.field.vis(VAR_OMEGA)[0]
+def dns_om2_phys(S: DnsState) -> None:
+    """Physical vorticity from om2 into ur_full[2] (turbo_simulator.py:2684-2687)."""
+    S.field.vis(VAR_OMEGA, out=S.ur_full.plane2())
 
 
-def dns_stream_func(S: DnsState):
-    """Streamfunction om2/(K2 + 1e-30) on the 3/2 grid (turbo_simulator.py:2690-2708)."""
-    return S.field.vis(VAR_STREAM)[0]
+def dns_stream_func(S: DnsState) -> None:
+    """Streamfunction om2/(K2 + 1e-30) on the 3/2 grid into ur_full[2] (turbo_simulator.py:2690-2708)."""
+    S.field.vis(VAR_STREAM, out=S.ur_full.plane2())
 
 
 def frame_pixels(S: DnsState, var: int = VAR_U):

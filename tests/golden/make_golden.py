@@ -2,7 +2,7 @@
 
 Run in a container that has the reference checked out (read-only is fine):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the reference checkout>
 
 It imports palinstrophy.turbo_simulator from that checkout, uses its own
 generator and its own FP32 CPU (NumPy/scipy.fft) step functions, and writes

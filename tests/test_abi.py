@@ -47,33 +47,59 @@ def test_null_handle_is_an_error_not_a_crash(built_lib):
         L.check(built_lib.pal_step3(None))
 
 
-@pytest.mark.parametrize("N,K0,seed", [(64, 10.0, 4895), (128, 15.0, 4895), (96, 12.0, 7)])
-def test_host_generator_km3_matches_oracle(built_lib, N, K0, seed):
-    """KM3 modes are computed in double, but their normalisation uses the PAO
-    energy, whose float32 exp/sin/cos come from libm here and from NumPy's own
-    float32 kernels in the reference: values agree to a few ulp (relative 3e-7), most exactly."""
-    om2, uc, st = L.pao_generate(N, K0, 1e4, seed, "KM3")
-    g = pg.generate(N, K0, 1e4, seed, "KM3")
-    fa, fb = uc.view(np.float32), g["uc_low"].view(np.float32)
-    assert (np.abs(fa - fb) <= 3e-7 * np.abs(fb)).all()
-    assert (fa == fb).mean() > 0.9
-    assert np.abs(om2 - g["om2"]).max() <= 3e-7 * np.abs(g["om2"]).max()
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.mark.parametrize("name", ["init_KM3_N64_s4895_k10", "init_KM3_N128_s4895_k15", "init_KM3_N256_s4895_k10",
+                                  "init_PAO_N128_s4895_k15", "init_PAO_N64_s7_k12"])
+def test_host_generator_is_the_reference_field(built_lib, name):
+    """The product generator (C++ LCG and shells, NumPy float32 cos/sin/exp) gives
+    the reference's own arrays bit for bit -- signs of zero modes included -- and
+    its printed Energy / WiWi and final seed."""
+    d = golden(name + ".npz")
+    om2, uc, st = L.pao_generate(int(d["N"]), float(d["K0"]), float(d["Re"]), int(d["seed"]), str(d["spectrum"]))
+    assert np.array_equal(_bits(om2), _bits(d["om2"]))
+    assert np.array_equal(_bits(uc), _bits(d["uc_low"]))
+    assert st["seed_out"] == int(d["seed_out"])
+    assert abs(st["Energy"] - float(d["Energy"])) <= 1e-8 * abs(float(d["Energy"]))
+    assert abs(st["WiWi"] - float(d["WiWi"])) <= 1e-7 * abs(float(d["WiWi"]))
+    assert np.float32(st["visc"]) == d["visc"]
+
+
+@pytest.mark.parametrize("N,K0,seed,spec", [(96, 12.0, 7, "KM3"), (160, 6.0, 11, "PAO"), (200, 20.0, 5010, "KM3")])
+def test_host_generator_matches_oracle_restatement(built_lib, N, K0, seed, spec):
+    """Sizes and seeds without a fixture: the product equals the oracle's scalar
+    restatement of the reference generator bit for bit, moments exactly."""
+    om2, uc, st = L.pao_generate(N, K0, 1e4, seed, spec)
+    g = pg.generate(N, K0, 1e4, seed, spec)
+    assert np.array_equal(_bits(om2), _bits(g["om2"]))
+    assert np.array_equal(_bits(uc), _bits(g["uc_low"]))
     assert st["seed_out"] == g["seed_out"]
-    assert abs(st["Energy"] - g["Q2"]) <= 1e-7 * g["Q2"]
-    assert np.float32(st["visc"]) == g["visc"]
+    assert st["Energy"] == g["Q2"] and st["WiWi"] == g["W2"]
 
 
-def test_host_generator_pao_close(built_lib):
-    """PAO uses float32 exp/sin/cos; libm and NumPy may differ in the last bit."""
+def test_libm_generator_close(built_lib):
+    """pal_pao_generate takes cos/sin/exp from the C library, which may differ
+    from NumPy's float32 ufuncs in the last bit: a few ulp, seeds exact."""
     d = golden("init_PAO_N64_s7_k12.npz")
-    om2, uc, st = L.pao_generate(64, 12.0, 1e4, 7, "PAO")
+    om2, uc, st = L.pao_generate_libm(64, 12.0, 1e4, 7, "PAO")
     assert st["seed_out"] == int(d["seed_out"])
     scale = np.abs(d["uc_low"]).max()
     assert np.abs(uc - d["uc_low"]).max() <= 4e-7 * scale
     assert np.abs(om2 - d["om2"]).max() <= 4e-7 * np.abs(d["om2"]).max()
     assert abs(st["Energy"] - float(d["Energy"])) < 1e-6
+    om2, uc, st = L.pao_generate_libm(128, 15.0, 1e4, 4895, "KM3")
+    g = golden("init_KM3_N128_s4895_k15.npz")
+    assert np.abs(uc - g["uc_low"]).max() <= 4e-7 * np.abs(g["uc_low"]).max()
 
 
 def test_host_generator_rejects_bad_n(built_lib):
     buf = np.zeros(16, np.complex64)
+    f = np.zeros(16, np.float32)
     assert built_lib.pal_pao_generate(30, 10.0, 1e4, 1, 0, L.ptr(buf), L.ptr(buf), None, None) == L.PAL_ERR_INVALID
+    assert built_lib.pal_pao_draws(30, 1, L.ptr(f), None) == L.PAL_ERR_INVALID
+    assert built_lib.pal_pao_build(64, 10.0, 1e4, 1, 0, None, L.ptr(f), L.ptr(f), L.ptr(buf), L.ptr(buf),
+                                   None) == L.PAL_ERR_INVALID
+    with pytest.raises(ValueError):
+        L.pao_generate(30, 10.0, 1e4, 1)

@@ -51,3 +51,43 @@ def test_warmup_is_raised_to_three(bench, monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--warmup", "1"])
     bench.main()
     assert seen["warmup"] == 3
+
+
+def test_reference_arm_loads_nothing_from_the_product():
+    """The reference arm builds its start with the oracle's restatement of the
+    reference generator and times the oracle's FP32 port: palinstrophy_gb300
+    (and its libpalgpu.so) is never imported."""
+    code = (
+        "import sys, types; sys.argv=['bench.py']; import bench; bench.N_GRID = 64; "
+        "bench.run_reference(types.SimpleNamespace(steps=2, gpus=1)); "
+        "bad = [m for m in sys.modules if m.startswith('palinstrophy_gb300')]; "
+        "assert not bad, bad; print('CLEAN')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    line = json.loads(out.stdout.strip().splitlines()[0])
+    assert line["impl"] == "reference" and line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["cores"] == min(8, os.cpu_count() or 1)
+    assert out.stdout.strip().endswith("CLEAN")
+
+
+def test_oracle_process_round_trip():
+    """The spawned FP64 oracle leg returns the final field and the NEXTDT log
+    (first row: the initial dt) of the same run done in-process."""
+    import numpy as np
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import bench  # importable by name, as the spawned child needs
+    from oracle import dns_oracle as do
+    from oracle import pao_generator as pg
+    g = pg.generate_fast(64, 10.0, 1e4, 4895, "KM3")
+    run = bench._OracleRun(g["om2"], g["uc_low"], float(g["visc"]), 5)
+    om2, log, secs, threads = run.result(timeout=300)
+    S = do.OracleState(64, g["om2"], g["uc_low"], float(g["visc"]), bench.CFL)
+    do.init_dt(S)
+    dt0 = S.dt
+    ref_log = []
+    do.run(S, 5, bench.METHOD, bench.UPDATE, log=ref_log)
+    assert np.array_equal(om2, S.om2)
+    assert log[0, 0] == dt0 and len(log) == 1 + len(ref_log)
+    assert [int(r[0]) for r in log[1:]] == [1, 5]
+    assert secs > 0 and threads >= 1

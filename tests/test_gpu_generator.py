@@ -77,8 +77,28 @@ def test_fp64_handle_gets_the_same_start(ts):
     assert np.array_equal(uc64, uc32.astype(np.complex128))
 
 
+@pytest.mark.parametrize("name", ["init_KM3_N64_s4895_k10", "init_KM3_N128_s4895_k15", "init_KM3_N256_s4895_k10",
+                                  "init_PAO_N128_s4895_k15", "init_PAO_N64_s7_k12"])
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_create_dns_state_starts_from_the_reference_field(ts, name, prec):
+    """The default create_dns_state path holds the reference's own initial arrays:
+    bit for bit equal to the fixtures the reference generated, and to the oracle's
+    restatement of the generator run on this machine."""
+    d = golden(name + ".npz")
+    N = int(d["N"])
+    S = ts.create_dns_state(N, float(d["Re"]), float(d["K0"]), 0.5, seed=int(d["seed"]),
+                            start_spectrum=str(d["spectrum"]), precision=prec)
+    om2 = S.om2
+    g = pg.generate_fast(N, float(d["K0"]), float(d["Re"]), int(d["seed"]), str(d["spectrum"]))
+    assert np.array_equal(om2, g["om2"].astype(om2.dtype))
+    assert np.array_equal(om2, d["om2"].astype(om2.dtype))
+    assert np.array_equal(S.uc_init, d["uc_low"])
+    assert S.visc == float(d["visc"])
+    S.field.close()
+
+
 def test_create_dns_state_device_generator_steps(ts):
-    S = ts.create_dns_state(128, 1e4, 15.0, 0.5, seed=4895, start_spectrum="KM3")
+    S = ts.create_dns_state(128, 1e4, 15.0, 0.5, seed=4895, start_spectrum="KM3", generator="device")
     ts._init_dt(S)
     S.field.step("LS_IMEX_RK3", 5, update=1)
     d = S.diagnostics()

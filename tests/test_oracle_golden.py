@@ -30,6 +30,25 @@ def test_generator_bit_exact(name):
     assert g["visc"] == d["visc"]
 
 
+@pytest.mark.parametrize("name", INITS + ["init_KM3_N256_s4895_k10"])
+def test_fast_generator_bit_exact(name):
+    """The vectorised restatement gives the fixtures bit for bit (signs of zeros too)."""
+    d = golden(name + ".npz")
+    g = pg.generate_fast(int(d["N"]), float(d["K0"]), float(d["Re"]), int(d["seed"]), str(d["spectrum"]))
+    assert np.array_equal(g["om2"].view(np.uint32), d["om2"].view(np.uint32))
+    assert np.array_equal(g["uc_low"].view(np.uint32), d["uc_low"].view(np.uint32))
+    assert g["seed_out"] == int(d["seed_out"])
+
+
+@pytest.mark.parametrize("N,K0,seed,spec", [(96, 12.0, 7, "KM3"), (160, 6.0, 11, "PAO"), (200, 20.0, 5010, "KM3")])
+def test_fast_generator_equals_scalar_restatement(N, K0, seed, spec):
+    a = pg.generate(N, K0, 1e4, seed, spec)
+    b = pg.generate_fast(N, K0, 1e4, seed, spec)
+    for k in ("om2", "uc_low"):
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    assert a["seed_out"] == b["seed_out"] and a["Q2"] == b["Q2"] and a["W2"] == b["W2"]
+
+
 def test_generator_known_answer_N256():
     """The printed init KAT: N=256 KM3 seed 4895 -> Energy 0.99681688, WiWi 384.68516, seed 4983."""
     d = golden("init_KM3_N256_s4895_k10.npz")
@@ -108,3 +127,27 @@ def test_oracle_flow_metrics_match_reference_log():
     row = d["log"][0]
     assert abs(U - row[5]) < 1e-5 * row[5]
     assert abs(Lh - row[6]) < 1e-5 * row[6]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_threaded_passes_equal_single_thread(dtype):
+    """The elementwise passes split over host threads give the same bits as one thread."""
+    N = 512
+    d = golden("init_KM3_N256_s4895_k10.npz")
+    rng = np.random.default_rng(3)
+    om2 = np.zeros((N, N // 2), np.complex64)
+    om2[:128, :128] = d["om2"][:128, :128]
+    om2[-128:, :128] = d["om2"][-128:, :128]
+    om2 += (1e-3 * (rng.standard_normal(om2.shape) + 1j * rng.standard_normal(om2.shape))).astype(np.complex64)
+    om2[0, 0] = 0
+    runs = []
+    for threads in (1, 8):
+        S = do.OracleState(N, om2, np.zeros((2, N, N // 2), np.complex64), d["visc"], 0.5, dtype=dtype,
+                           threads=threads)
+        do.reconstruct_velocity(S)
+        do.init_dt(S)
+        do.rk3(S)
+        do.cnab2(S)
+        runs.append((S.om2, S.fnm1, S.ur_full))
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)

@@ -36,7 +36,9 @@ enum {
   PAL_ERR_CUDA = -2,        /* a CUDA runtime call failed */
   PAL_ERR_OOM = -3,         /* device allocation failed */
   PAL_ERR_STATE = -4,       /* call out of order (e.g. step3 before step2b) */
-  PAL_ERR_NONFINITE = -5    /* NaN/Inf detected in the field */
+  PAL_ERR_NONFINITE = -5,   /* NaN/Inf detected in the field */
+  PAL_ERR_TIMEOUT = -6      /* a kernel's bounded wait for its own bulk copies ran out (reported by the
+                               next call that reads the device scalars, which clears it) */
 };
 
 enum { PAL_FP32 = 0, PAL_FP64 = 1 };
@@ -168,6 +170,14 @@ int pal_set_variant(pal_handle* h, int row, int col);
 /* Resident blocks per SM of the selected row and column kernels, from the CUDA
  * occupancy calculator (diagnostic; no counterpart in the reference). */
 int pal_get_occupancy(pal_handle* h, int* row_blocks_per_sm, int* col_blocks_per_sm);
+/* Test switches (no counterpart in the reference).  PAL_DBG_SKIP_FIRST_WAIT,
+ * value 1: the kernels that move tiles by TMA give their first wait for the
+ * tile's bulk copies no polls, so they take the path that reports a timed-out
+ * wait (PAL_ERR_TIMEOUT from the next pal_get_scalars / pal_compute_cflm /
+ * pal_diagnostics), then wait for the copies with the normal bound before using
+ * the tile; the results stay valid.  Value 0 restores the normal waits. */
+enum { PAL_DBG_SKIP_FIRST_WAIT = 0 };
+int pal_set_debug(pal_handle* h, int what, int value);
 /* The handle's CUDA stream (cudaStream_t), for event timing or interop. */
 int pal_get_stream(pal_handle* h, void** stream);
 int pal_last_error(pal_handle* h, char* buf, size_t n);

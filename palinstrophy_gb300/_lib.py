@@ -22,6 +22,8 @@ PAL_ERR_CUDA = -2
 PAL_ERR_OOM = -3
 PAL_ERR_STATE = -4
 PAL_ERR_NONFINITE = -5
+PAL_ERR_TIMEOUT = -6
+PAL_DBG_SKIP_FIRST_WAIT = 0
 PAL_FP32, PAL_FP64 = 0, 1
 PAL_CNAB2, PAL_LS_IMEX_RK3 = 0, 1
 PAL_FIELD_OM2, PAL_FIELD_FNM1, PAL_FIELD_UR_U, PAL_FIELD_UR_V = 0, 1, 2, 3
@@ -75,6 +77,7 @@ _SIGS = {
     "pal_materialize_physical": (_I, [_H]),
     "pal_synchronize": (_I, [_H]),
     "pal_get_stream": (_I, [_H, ctypes.POINTER(_P)]),
+    "pal_set_debug": (_I, [_H, _I, _I]),
     "pal_get_variant": (_I, [_H, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                              ctypes.c_char_p, ctypes.c_size_t]),
     "pal_set_variant": (_I, [_H, _I, _I]),

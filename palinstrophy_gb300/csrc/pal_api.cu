@@ -62,6 +62,7 @@ struct pal_handle {
   bool vel_uploaded = false;  // ST_VEL_PENDING source: stage buffer (true) or om inversion
   long long it = 0;           // host copy of the iteration counter
   int spectral_blocks = 0;
+  int dbg_wait0 = 0;          // pal_set_debug(PAL_DBG_SKIP_FIRST_WAIT)
   std::string err;
 };
 
@@ -164,6 +165,7 @@ StepArgs base_args(pal_handle* h) {
   a.tmaps = &h->tmaps;
   a.cmaps = &h->cmaps;
   a.N = h->N;
+  a.dbg_wait0 = h->dbg_wait0;
   return a;
 }
 
@@ -232,7 +234,7 @@ int read_scalars(pal_handle* h) {
                     cudaMemcpyHostToDevice, h->stream);
     cudaStreamSynchronize(h->stream);
     h->sc_host->wait_timeout = 0;
-    return fail(h, PAL_ERR_CUDA, "a device wait for bulk copies timed out; the last steps are not valid");
+    return fail(h, PAL_ERR_TIMEOUT, "a device wait for bulk copies timed out; the last steps are not valid");
   }
   return PAL_OK;
 }
@@ -1103,6 +1105,16 @@ int pal_set_variant(pal_handle* h, int row, int col) {
   if (int rc = check(h)) return rc;
   if (h->state == ST_P) return fail(h, PAL_ERR_STATE, "change kernels between steps, not between step2b and step3");
   return select_variant(h, row, col);
+}
+
+int pal_set_debug(pal_handle* h, int what, int value) {
+  if (int rc = check(h)) return rc;
+  if (what != PAL_DBG_SKIP_FIRST_WAIT || (value != 0 && value != 1))
+    return fail(h, PAL_ERR_INVALID, "unknown debug switch or value");
+  h->dbg_wait0 = value;
+  for (auto& kv : h->step_graphs) cudaGraphExecDestroy(kv.second);  // they hold the old kernel arguments
+  h->step_graphs.clear();
+  return PAL_OK;
 }
 
 int pal_get_stream(pal_handle* h, void** stream) {

@@ -75,6 +75,10 @@ struct StepArgs {
   void* fm_p;
   const struct TmaMaps* tmaps;  // host: descriptors of w0 / w1 for the row pass's bulk copies
   const struct TmaMaps* cmaps;  // host: descriptors of w0 / w1 for the column pass's bulk copies
+  // Test switch: 1 gives the first bounded wait for a tile's bulk copies no polls,
+  // so the kernel takes its report path (wait_timeout) and then waits for the
+  // copies with the normal bound before it uses the tile.
+  int dbg_wait0;
 };
 
 // Rows per TMA box of the row tiles: the largest power of two up to 256 that
@@ -423,7 +427,7 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
       tma_load_3d(&maps.w1, sm + (size_t)(Nh + bx * BOX) * V, bar, 2 * z0, bx * BOX, (int)blockIdx.y);
     }
   }
-  if (!mbar_wait(bar, 0, 1 << 22)) {
+  if (!mbar_wait(bar, 0, a.dbg_wait0 ? 0 : 1 << 22)) {
     // the copies did not complete in time: report it and wait (bounded) for them
     // before the shared memory is used or released
     if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
@@ -1244,7 +1248,7 @@ __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_
   }
   const ModeCoef<T> cf = col_coef<T>(a, N);
   __syncthreads();  // every thread sees the initialised barrier
-  if (!mbar_test_wait(&bar, 0, 1 << 20)) {
+  if (!mbar_test_wait(&bar, 0, a.dbg_wait0 ? 0 : 1 << 20)) {
     // the copies did not complete in time: report it and wait (bounded) for them
     // before the shared memory is used or released
     if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);

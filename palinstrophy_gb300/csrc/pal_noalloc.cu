@@ -22,6 +22,9 @@
 //     first call before any stream capture begins.
 //   - Calls are asynchronous on `stream` (null = the legacy default stream);
 //     om2/fnm1 hold the result once that stream's work has finished.
+//   - Launch errors are read with cudaPeekAtLastError, which leaves the
+//     thread's pending CUDA error in place: an error raised earlier by the
+//     caller's own code is reported here as PAL_ERR_CUDA but not cleared.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -107,6 +110,7 @@ extern "C" int pal_step_noalloc(int N, int method, int nsteps, double dt, double
   void* tw_row = base + kOffTwiddles;
   void* tw_col = base + kOffTwiddles + tw_half;
   k_noalloc_init<<<1, 32, 0, s>>>(a.sc, dt, visc, cn, cnm1);
+  if (cudaPeekAtLastError() != cudaSuccess) return PAL_ERR_CUDA;
   rk.twiddles(tw_row, s);
   ck.twiddles(tw_col, s);
   ks->transpose(om2, a.om, N, Nh, 1, s);      // caller layout (N, N/2) -> [kx][z]
@@ -142,5 +146,5 @@ extern "C" int pal_step_noalloc(int N, int method, int nsteps, double dt, double
   }
   ks->transpose(a.om, om2, Nh, N, 1, s);      // back to the caller's layout
   ks->transpose(a.fnm1, fnm1, Nh, N, 1, s);
-  return cudaGetLastError() == cudaSuccess ? PAL_OK : PAL_ERR_CUDA;
+  return cudaPeekAtLastError() == cudaSuccess ? PAL_OK : PAL_ERR_CUDA;
 }

@@ -195,6 +195,10 @@ class Field:
     def set_variant(self, row: int, col: int):
         self._ck(self.lib.pal_set_variant(self.h, int(row), int(col)))
 
+    def set_debug(self, what: int, value: int):
+        """Test switch (pal_set_debug), e.g. L.PAL_DBG_SKIP_FIRST_WAIT."""
+        self._ck(self.lib.pal_set_debug(self.h, int(what), int(value)))
+
     def stream_ptr(self) -> int:
         p = L._P()
         self._ck(self.lib.pal_get_stream(self.h, L.ctypes.byref(p)))

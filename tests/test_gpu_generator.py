@@ -3,6 +3,8 @@ fields (committed fixtures) and against the host restatement.  Float32
 exp/sin/cos (and double sin/cos) come from CUDA's library here, from NumPy in
 the reference and libm in the host restatement, so values agree to a few ulp,
 as the host restatement's do; seeds, shells and the mode set are exact."""
+import platform
+
 import numpy as np
 import pytest
 
@@ -81,18 +83,26 @@ def test_fp64_handle_gets_the_same_start(ts):
                                   "init_PAO_N128_s4895_k15", "init_PAO_N64_s7_k12"])
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 def test_create_dns_state_starts_from_the_reference_field(ts, name, prec):
-    """The default create_dns_state path holds the reference's own initial arrays:
-    bit for bit equal to the fixtures the reference generated, and to the oracle's
-    restatement of the generator run on this machine."""
+    """The default create_dns_state path holds the reference generator's arrays as
+    the reference computes them on this machine: bit for bit equal to the oracle's
+    scalar restatement of the generator (NumPy float32 scalars, as the reference)
+    run here.  The fixtures were made by the reference on x86-64, and NumPy's
+    float32 cos/sin/exp kernels differ between CPU architectures in the last bit,
+    so against them the arrays are bit-exact on x86-64 (also checked without a GPU
+    in tests/test_abi.py) and within a few ulp elsewhere."""
     d = golden(name + ".npz")
     N = int(d["N"])
     S = ts.create_dns_state(N, float(d["Re"]), float(d["K0"]), 0.5, seed=int(d["seed"]),
                             start_spectrum=str(d["spectrum"]), precision=prec)
     om2 = S.om2
-    g = pg.generate_fast(N, float(d["K0"]), float(d["Re"]), int(d["seed"]), str(d["spectrum"]))
+    g = pg.generate(N, float(d["K0"]), float(d["Re"]), int(d["seed"]), str(d["spectrum"]))
     assert np.array_equal(om2, g["om2"].astype(om2.dtype))
-    assert np.array_equal(om2, d["om2"].astype(om2.dtype))
-    assert np.array_equal(S.uc_init, d["uc_low"])
+    assert np.array_equal(S.uc_init.view(np.uint32), g["uc_low"].view(np.uint32))
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert np.array_equal(S.uc_init.view(np.uint32), d["uc_low"].view(np.uint32))
+    else:
+        assert np.abs(S.uc_init - d["uc_low"]).max() <= 4e-7 * np.abs(d["uc_low"]).max()
+        assert np.abs(om2 - d["om2"]).max() <= 4e-7 * np.abs(d["om2"]).max()
     assert S.visc == float(d["visc"])
     S.field.close()
 

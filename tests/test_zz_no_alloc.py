@@ -15,7 +15,6 @@ import ctypes
 import numpy as np
 import pytest
 
-from conftest import golden
 from oracle import dns_oracle as do
 
 pytestmark = pytest.mark.gpu
@@ -45,14 +44,26 @@ def _reference_path(Field, om2, fnm1, method, nsteps, dt, visc, cn, cnm1):
     return out
 
 
+def _start(Field, L, N):
+    """A KM3 start at N and a fixed dt at CFL 0.5 for it."""
+    import math
+    om2, uc, st = L.pao_generate(N, 10.0, 1e4, 4895, "KM3")
+    F = Field(N, "fp32", 1e4, 0.5)
+    F.set_state(om2, None, uc)
+    F.step2a()
+    dt = 0.5 / (F.compute_cflm() * math.pi)
+    F.close()
+    return om2.astype(np.complex64), float(st["visc"]), dt
+
+
+@pytest.mark.parametrize("N", [32, 256, 512])
 @pytest.mark.parametrize("method,code", [("CNAB2", 0), ("LS_IMEX_RK3", 1)])
-def test_two_calls_match_allocating_path(env, method, code):
+def test_two_calls_match_allocating_path(env, method, code, N):
+    """Both ends of the supported range (N=512 is the largest field the scratch
+    holds) and a middle size, each method; the second call allocates nothing."""
     torch, L, Field = env
-    d = golden("init_KM3_N256_s4895_k10.npz")
-    N = 256
-    om2 = d["om2"].astype(np.complex64)
+    om2, visc, dt = _start(Field, L, N)
     fnm1 = np.zeros_like(om2)
-    visc, dt = float(d["visc"]), 1e-3  # CFL about 0.5 at this N
     lib = L.load()
     dom = torch.from_numpy(om2.copy()).cuda()
     dfn = torch.from_numpy(fnm1.copy()).cuda()
@@ -65,10 +76,14 @@ def test_two_calls_match_allocating_path(env, method, code):
     a_om, a_fn = _reference_path(Field, om2, fnm1, method, 3, dt, visc, 1.0, 0.0)
     assert do.rel_l2(a_om, dom.cpu().numpy()) <= TOL
     assert do.rel_l2(a_fn, dfn.cpu().numpy()) <= TOL
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
     rc = lib.pal_step_noalloc(N, code, 4, dt, visc, 1.0, 1.0 if method == "CNAB2" else 0.0,
                               ctypes.c_void_p(dom.data_ptr()), ctypes.c_void_p(dfn.data_ptr()), stream)
-    assert rc == L.PAL_OK
     torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert rc == L.PAL_OK
+    assert free_after == free_before, (free_before, free_after)   # no device memory taken
     b_om, b_fn = _reference_path(Field, om2, fnm1, method, 7, dt, visc, 1.0, 0.0)
     assert do.rel_l2(b_om, dom.cpu().numpy()) <= TOL
     assert do.rel_l2(b_fn, dfn.cpu().numpy()) <= TOL

@@ -157,6 +157,48 @@ def _limiter(kernel, prec):
             f"FP32 FMA pipe {fma} (profiles/{kernel}_{prec}_N{N_GRID}.md)")
 
 
+def _fp64_flops(kernel):
+    """FP64 flops per launch (2 x DFMA + DADD + DMUL thread instructions) of the
+    FP64 plain path's kernel at N=4096, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"kernels_fp64_N{N_GRID}.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith(f"fp64_flops_per_launch_{kernel}:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def _fp64_roofline(om2, uc, visc):
+    """The FP64 plain path against its own ceiling: counted FP64 flops per k_row /
+    k_col launch (ncu instruction counts, profiles/) over the launch times measured
+    here, against the FP64 FMA throughput measured here (pal_fp64_peak); and the
+    same launches' algorithmic bytes against the measured HBM bandwidth."""
+    from palinstrophy_gb300 import _lib as L
+    F = _field("fp64", om2, uc, visc)
+    ms_row, ms_col, _ = F.profile_kernels(METHOD, 2)
+    desc = F.variant()["desc"]
+    F.close()
+    peak, peak_ms = L.fp64_peak()
+    hbm, _ = _peaks()
+    n2 = float(N_GRID) * N_GRID
+    out = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak,
+           "peak_kind": f"measured: FP64 FMA-chain microbenchmark (pal_fp64_peak, {peak_ms:.1f} ms launch)",
+           "kernels": desc}
+    for name, ms, nbytes in (("k_row", ms_row, 6.0 * n2 * 8), ("k_col", ms_col, (25.0 / 3.0) * n2 * 8)):
+        fl = _fp64_flops(name)
+        ach = fl / (ms / 1000.0) / 1e12 if fl else None
+        out[name] = {"ms": ms, "flops_per_launch": fl, "achieved": ach, "frac": ach / peak if ach else None,
+                     "hbm_GBps": nbytes / (ms / 1000.0) / 1e9, "hbm_frac": nbytes / (ms / 1000.0) / 1e9 / hbm}
+    dom = "k_row" if ms_row >= ms_col else "k_col"
+    out["kernel"] = dom
+    out["achieved"] = out[dom]["achieved"]
+    out["frac"] = out[dom]["frac"]
+    return out
+
+
 def _init_arrays():
     from palinstrophy_gb300 import _lib as L
     return L.pao_generate(N_GRID, K0, RE, SEED, "KM3")
@@ -641,6 +683,7 @@ def run_gb300(args):
 
     e2e_rate, h2d, d2h = _e2e("fp32", om2, uc, visc, args.steps)
     oracle = _OracleRun(om2, uc, visc, 100)
+    fp64_roof = _fp64_roofline(om2, uc, visc)
     ens = _ensemble_rate()
     diff = _differentiation()
     prec_form = _precision_form()
@@ -703,6 +746,7 @@ def run_gb300(args):
                                    f"numpy/scipy.fft port of the reference path, scipy.fft workers={cpu_workers} "
                                    f"(the reference's min(8, cores)), {_cpu_name()}"},
         "clocks": clocks,
+        "fp64_roofline": fp64_roof,
         "fp64": {"value": rate64, "unit": "steps/s", "steps": k64, "ms_per_step": ms64 / k64},
         "fp32_over_fp64": rate32 / rate64,
         "rel_l2_fp32_vs_fp64_100_steps": rel,

@@ -79,7 +79,8 @@ int pal_device_info(int* sm_count, int* smem_optin, char* name, size_t name_len)
 /* Initial state as create_dns_state leaves it (turbo_simulator.py:1191-1234):
  * om2 and fnm1 (fnm1 may be NULL for zeros), and the velocity low band that
  * the first dns_step2a transforms (uc_low may be NULL: then the velocity is
- * rebuilt from om2 by the inversion of turbo_simulator.py:1555-1585). */
+ * rebuilt from om2 by the inversion of turbo_simulator.py:1555-1585).  The
+ * arrays may be in host or device memory (copied with unified addressing). */
 int pal_set_spectral_state(pal_handle* h, const void* om2, const void* fnm1);
 int pal_set_velocity_spectrum(pal_handle* h, const void* uc_low);
 
@@ -158,6 +159,11 @@ int pal_synchronize(pal_handle* h);
  * milliseconds, and the number of kernels launched.  Measurement support; no
  * counterpart in the reference. */
 int pal_profile_kernels(pal_handle* h, int method, int nsteps, double* ms_row, double* ms_col, int* launches);
+/* FP64 FMA throughput of the current GPU in TFLOP/s (best of 5 timed launches of
+ * an FMA-chain kernel filling every SM, CUDA events; *ms = that launch's time):
+ * the ceiling of the FP64 plain path, whose kernels are bound by the FP64 pipe.
+ * Measurement support; no counterpart in the reference. */
+int pal_fp64_peak(double* tflops, double* ms);
 /* Kernel candidates: for each N the library compiles several row-pass and
  * column-pass kernels (radix order, rows per tile, threads per block).
  * pal_create times them on the new handle and keeps the fastest, once per

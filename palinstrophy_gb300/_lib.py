@@ -78,6 +78,7 @@ _SIGS = {
     "pal_synchronize": (_I, [_H]),
     "pal_get_stream": (_I, [_H, ctypes.POINTER(_P)]),
     "pal_set_debug": (_I, [_H, _I, _I]),
+    "pal_fp64_peak": (_I, [_DP, _DP]),
     "pal_get_variant": (_I, [_H, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                              ctypes.c_char_p, ctypes.c_size_t]),
     "pal_set_variant": (_I, [_H, _I, _I]),
@@ -203,3 +204,10 @@ def pao_generate_libm(N, K0, Re, seed, spectrum="KM3"):
     check(load().pal_pao_generate(int(N), float(K0), float(Re), int(seed), spec, ptr(om2), ptr(uc), st,
                                   ctypes.byref(so)))
     return om2, uc, {"Energy": st[0], "WiWi": st[1], "visc": st[2], "seed_out": so.value}
+
+
+def fp64_peak():
+    """(TFLOP/s, ms) of the FP64 FMA microbenchmark on the current GPU (pal_fp64_peak)."""
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    check(load().pal_fp64_peak(ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value, ms.value

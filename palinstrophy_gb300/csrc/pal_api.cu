@@ -109,7 +109,7 @@ bool encode_col_maps(TmaMaps* out, void* w0, void* w1, int N, int RP, int member
   const cuuint64_t strides[2] = {(cuuint64_t)RP * 8, (cuuint64_t)M * 8};  // bytes, dims 1 and 2
   // the box's inner extent (2 RP + 4 floats) runs past the 2 RP floats of a
   // group: loads fill those 4 floats with zeros, stores leave them out
-  const cuuint32_t box[3] = {(cuuint32_t)(2 * RP + 4), (cuuint32_t)(G < 256 ? G : 256), 1};
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * RP + 4), (cuuint32_t)pal::col_box_groups(G), 1};
   const cuuint32_t elem[3] = {1, 1, 1};
   void* base[2] = {w0, w1};
   CUtensorMap* maps[2] = {&out->w0, &out->w1};
@@ -496,11 +496,12 @@ int pal_set_spectral_state(pal_handle* h, const void* om2, const void* fnm1) {
   if (int rc = check(h)) return rc;
   if (!om2) return fail(h, PAL_ERR_INVALID, "om2 is null");
   const size_t bytes = (size_t)h->N * h->Nh * h->esz;
-  PAL_CK(h, cudaMemcpyAsync(h->stage, om2, bytes, cudaMemcpyHostToDevice, h->stream));
+  // cudaMemcpyDefault: om2 / fnm1 may be host or device memory (unified addressing)
+  PAL_CK(h, cudaMemcpyAsync(h->stage, om2, bytes, cudaMemcpyDefault, h->stream));
   h->ks->transpose(h->stage, h->om, h->N, h->Nh, 1, h->stream);
   PAL_LAUNCHED(h, "transpose om2");
   if (fnm1) {
-    PAL_CK(h, cudaMemcpyAsync(h->stage, fnm1, bytes, cudaMemcpyHostToDevice, h->stream));
+    PAL_CK(h, cudaMemcpyAsync(h->stage, fnm1, bytes, cudaMemcpyDefault, h->stream));
     h->ks->transpose(h->stage, h->fnm1, h->N, h->Nh, 1, h->stream);
     PAL_LAUNCHED(h, "transpose fnm1");
   } else {
@@ -539,7 +540,7 @@ int pal_set_velocity_spectrum(pal_handle* h, const void* uc_low) {
     return PAL_OK;
   }
   const size_t bytes = 2 * (size_t)h->N * h->Nh * h->esz;
-  PAL_CK(h, cudaMemcpyAsync(h->stage, uc_low, bytes, cudaMemcpyHostToDevice, h->stream));
+  PAL_CK(h, cudaMemcpyAsync(h->stage, uc_low, bytes, cudaMemcpyDefault, h->stream));
   PAL_CK(h, cudaStreamSynchronize(h->stream));
   h->state = ST_VEL_PENDING;
   h->vel_uploaded = true;

@@ -25,7 +25,10 @@ const RowKernels r4096[] = {RowOf<float, P6144, 4, 512>::make("16.16.24 V4x512")
                             RowOf<float, RecT<P6144>, 2, 384, 31>::make("16.16.24t V2x384 tma-in tma-out l2pf"),
                             RowOf<float, RecT<P6144>, 2, 384, 63>::make("16.16.24t V2x384 tma-in tma-out l2pf2"),
                             RowOf<float, RecT<P6144>, 2, 384, 30>::make("16.16.24t V2x384 tma-in tma-out"),
-                            RowOf<float, Rec<P6144>, 2, 384, 30>::make("16.16.24r V2x384 tma-in tma-out")};
+                            RowOf<float, Rec<P6144>, 2, 384, 30>::make("16.16.24r V2x384 tma-in tma-out"),
+                            RowOf<float, Rec<P6144c>, 2, 256, 30>::make("24.16.16r V2x256 tma-in tma-out"),
+                            RowOf<float, RecT<P6144c>, 2, 256, 30>::make("24.16.16t V2x256 tma-in tma-out"),
+                            RowOf<float, Rec<P6144d>, 2, 384, 30>::make("16.24.16r V2x384 tma-in tma-out")};
 const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
                             ColOf<float, Rec<P6144c>, 256>::make("24.16.16r x256"),
                             ColOf<float, Rec<P6144>, 256>::make("16.16.24r x256"),
@@ -37,7 +40,9 @@ const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
                             ColOf<float, Rec<P6144c>, 256, 3>::make("24.16.16r x256 hoist pipe0"),
                             ColOf<float, RecT<P6144>, 256, 3>::make("16.16.24t x256 hoist pipe0"),
                             ColOf<float, RecT<P6144d>, 256, 3>::make("16.24.16t x256 hoist pipe0"),
-                            ColOf<float, Rec<P6144>, 256, 4>::make("16.16.24r x256 tma")};
+                            ColOf<float, Rec<P6144>, 256, 4>::make("16.16.24r x256 tma"),
+                            ColOf<float, Rec<P6144c>, 256, 4>::make("24.16.16r x256 tma"),
+                            ColOf<float, Rec<P6144d>, 256, 4>::make("16.24.16r x256 tma")};
 
 PAL_KERNEL_SET(float, 0, 4096, r4096, c4096)
 }  // namespace

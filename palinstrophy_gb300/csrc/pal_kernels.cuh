@@ -83,6 +83,14 @@ struct StepArgs {
 
 // Rows per TMA box of the row tiles: the largest power of two up to 256 that
 // divides the N/2 stored rows (box dimensions are at most 256).
+// Groups per TMA box of the planar column tile: the largest divisor of the
+// group count g that is at most 256 (a box dimension's limit).
+__host__ __device__ constexpr int col_box_groups(int g) {
+  int b = g < 256 ? g : 256;
+  while (b > 1 && g % b != 0) --b;
+  return b;
+}
+
 __host__ __device__ constexpr int tma_box_rows(int nh) {
   int b = 256;
   while (b > 1 && nh % b != 0) b /= 2;
@@ -161,6 +169,59 @@ __device__ __forceinline__ double block_max(double m, double* red, int tid) {
   return m;
 }
 
+// Compensated FP64 summation: s + c carries the running sum, c the exact
+// rounding errors of the additions into s (TwoSum, which needs no ordering of
+// the operands' magnitudes).
+__device__ __forceinline__ void csum_add(double& s, double& c, double x) {
+  const double t = s + x;
+  const double bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
+
+// Block-wide compensated sum of K pairs (s, c): every level of the tree adds
+// the s parts with TwoSum and the c parts plainly.  Threads 0..31 hold s + c
+// in s on return.
+template <int NT, int K>
+__device__ __forceinline__ void block_csum(double (&s)[K], double (&c)[K], double* red /* 2*K*NT/32 */, int tid) {
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double so = __shfl_xor_sync(0xffffffffu, s[q], off);
+      const double co = __shfl_xor_sync(0xffffffffu, c[q], off);
+      csum_add(s[q], c[q], so);
+      c[q] += co;
+    }
+  }
+  constexpr int NW = NT / 32;
+  if ((tid & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      red[(2 * q) * NW + (tid >> 5)] = s[q];
+      red[(2 * q + 1) * NW + (tid >> 5)] = c[q];
+    }
+  }
+  __syncthreads();
+  if (tid < 32) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      double ss = tid < NW ? red[(2 * q) * NW + tid] : 0.0;
+      double cc = tid < NW ? red[(2 * q + 1) * NW + tid] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double so = __shfl_xor_sync(0xffffffffu, ss, off);
+        const double co = __shfl_xor_sync(0xffffffffu, cc, off);
+        csum_add(ss, cc, so);
+        cc += co;
+      }
+      s[q] = ss + cc;
+      c[q] = 0.0;
+    }
+  }
+  __syncthreads();
+}
+
 // Returns true in every thread of the block that finished last.
 __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
   __shared__ int is_last;
@@ -175,13 +236,15 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
 }
 
 // Physical-space statistics of one block: (max |u|+|v|, sum u^2+v^2) -> partials;
-// the last block reduces all partials in a fixed order and applies NEXTDT.
+// the last block reduces all partials in a fixed order and applies NEXTDT.  The
+// sum arrives as a thread's compensated pair (sum, comp) and stays compensated
+// through the block tree and the reduction of the partials.
 template <int NT>
-__device__ void finish_stats(const StepArgs& a, double mx, double sum, int M, int tid) {
+__device__ void finish_stats(const StepArgs& a, double mx, double sum, double comp, int M, int tid) {
   __shared__ double red[2 * (NT / 32)];
   mx = block_max<NT>(mx, red, tid);
-  double s1[1] = {sum};
-  block_sum<NT, 1>(s1, red, tid);
+  double s1[1] = {sum}, c1[1] = {comp};
+  block_csum<NT, 1>(s1, c1, red, tid);
   if (tid == 0) {
     a.part[2 * blockIdx.x] = mx;
     a.part[2 * blockIdx.x + 1] = s1[0];
@@ -189,13 +252,13 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, int M, in
   const bool last = last_block(&a.sc->row_counter, tid);
   if (!last) return;
   const int nb = gridDim.x;
-  double m2 = 0.0, s2[1] = {0.0};
+  double m2 = 0.0, s2[1] = {0.0}, c2[1] = {0.0};
   for (int q = tid; q < nb; q += NT) {
     m2 = fmax(m2, __ldcg(a.part + 2 * q));
-    s2[0] += __ldcg(a.part + 2 * q + 1);
+    csum_add(s2[0], c2[0], __ldcg(a.part + 2 * q + 1));
   }
   m2 = block_max<NT>(m2, red, tid);
-  block_sum<NT, 1>(s2, red, tid);
+  block_csum<NT, 1>(s2, c2, red, tid);
   if (tid == 0) {
     DevScalars* sc = a.sc;
     const double cflm = m2 * (double(a.N) / (2.0 * kPi));
@@ -692,7 +755,8 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
 
   // middle: last inverse DIF pass -> products -> first forward DIT pass
   const bool stats = (a.flags & F_STATS) != 0;
-  T mx = T(0), acc = T(0), comp = T(0);
+  T mx = T(0);
+  double acc = 0.0, comp = 0.0;  // compensated FP64 sum of u^2 + v^2
   {
     constexpr int R = PL::RP;
     constexpr int NB = V * (M / R);
@@ -705,15 +769,15 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
       for (int j = 0; j < R; ++j) x[j] = p[j * V];
       Dft<R, +1, C>::run(x);
       if (stats) {
+        double b = 0.0;  // this butterfly's R points, squares in FP64
 #pragma unroll
         for (int j = 0; j < R; ++j) {
           const T u = x[j].x, q = x[j].y;
           mx = fmax(mx, fabs(u) + fabs(q));
-          const T y = (u * u + q * q) - comp;  // Kahan
-          const T t = acc + y;
-          comp = (t - acc) - y;
-          acc = t;
+          const double du = double(u), dq = double(q);
+          b = fma(du, du, fma(dq, dq, b));
         }
+        csum_add(acc, comp, b);
       }
 #pragma unroll
       for (int j = 0; j < R; ++j) {
@@ -747,7 +811,7 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
       w1[(size_t)k * M + z0 + v] = C{T(0.5) * (p.y + q.y), T(-0.5) * (p.x - q.x)};
     }
   }
-  if (stats) finish_stats<NT>(a, double(mx), double(acc) - double(comp), M, tid);
+  if (stats) finish_stats<NT>(a, double(mx), acc, comp, M, tid);
 }
 
 // k_phys: U-state rows -> physical u, v (statistics, optional plane store).
@@ -763,7 +827,8 @@ __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
   dif_range<T, PL, V, NT, +1, 1, PL::NP>(sm, tw, tid);
-  T mx = T(0), acc = T(0), comp = T(0);
+  T mx = T(0);
+  double acc = 0.0, comp = 0.0;  // compensated FP64 sum of u^2 + v^2
   T* __restrict__ ph = static_cast<T*>(a.phys);
   const bool store = (a.flags & F_PHYS) != 0;
   for (int w = tid; w < V * M; w += NT) {
@@ -771,17 +836,15 @@ __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
     const int pos = w / V;
     const C val = sm[PL::phys(pos) * V + v];
     mx = fmax(mx, fabs(val.x) + fabs(val.y));
-    const T y = (val.x * val.x + val.y * val.y) - comp;
-    const T t = acc + y;
-    comp = (t - acc) - y;
-    acc = t;
+    const double du = double(val.x), dq = double(val.y);
+    csum_add(acc, comp, fma(du, du, dq * dq));
     if (store) {
       const int n = PL::freq(pos);
       ph[(size_t)(z0 + v) * M + n] = val.x;
       ph[(size_t)M * M + (size_t)(z0 + v) * M + n] = val.y;
     }
   }
-  finish_stats<NT>(a, double(mx), double(acc) - double(comp), M, tid);
+  finish_stats<NT>(a, double(mx), acc, comp, M, tid);
 }
 
 // --------------------------------------------------------------------------
@@ -844,7 +907,7 @@ struct ColPlanar {
   static constexpr int PADM = PL::M + 2 * (PL::M / RP);         // slots per plane
   static constexpr int PB = ((PADM * 8 + 127) / 128) * 128 / 8;  // plane stride (FP32 complex)
   static constexpr int G = PL::M / RP;                          // groups per plane
-  static constexpr int GBOX = G < 256 ? G : 256;                // groups per TMA box
+  static constexpr int GBOX = col_box_groups(G);                // groups per TMA box
   static __device__ __forceinline__ int phys(int k) { return k + 2 * (k / RP); }
   static constexpr int pstride(int p) { return PL::stride(p) == 1 ? 1 : PL::stride(p) + 2 * (PL::stride(p) / RP); }
   static constexpr bool fits = PL::M % RP == 0 && G % GBOX == 0 && (2 * RP + 4) * 4 % 16 == 0;  // whole groups, boxes
@@ -1399,7 +1462,8 @@ __global__ void __launch_bounds__(NT) k_spectral(StepArgs a0) {
   const int N = a.N, Nh = N >> 1;
   const long long total = (long long)N * Nh;
   const int tid = threadIdx.x;
-  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  // compensated FP64 sums: E, L numerator, Z (all modes), P, and the (0,0) mode
+  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, c[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   int bad = 0;
   for (long long idx = (long long)blockIdx.x * NT + tid; idx < total; idx += (long long)gridDim.x * NT) {
     const int kx = int(idx / N);
@@ -1412,28 +1476,28 @@ __global__ void __launch_bounds__(NT) k_spectral(StepArgs a0) {
     const double wt = (kx == 0 || kx == Nh - 1) ? 1.0 : 2.0;
     if (K2 > 0.0) {
       const double e = wt * p / K2;
-      s[0] += e;
-      s[1] += e / sqrt(K2);
+      csum_add(s[0], c[0], e);
+      csum_add(s[1], c[1], e / sqrt(K2));
     } else {
-      s[4] += p;  // the (0,0) mode, removed from Z
+      csum_add(s[4], c[4], p);  // the (0,0) mode, removed from Z
     }
-    s[2] += wt * p;
-    s[3] += wt * K2 * p;
+    csum_add(s[2], c[2], wt * p);
+    csum_add(s[3], c[3], wt * K2 * p);
   }
-  __shared__ double red[5 * (NT / 32)];
-  block_sum<NT, 5>(s, red, tid);
+  __shared__ double red[2 * 5 * (NT / 32)];
+  block_csum<NT, 5>(s, c, red, tid);
   if (bad) atomicOr(&a.sc->nonfinite, 1);
   if (tid == 0) {
 #pragma unroll
     for (int q = 0; q < 5; ++q) a.part[5 * blockIdx.x + q] = s[q];
   }
   if (!last_block(&a.sc->diag_counter, tid)) return;
-  double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0}, tc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int q = tid; q < (int)gridDim.x; q += NT) {
 #pragma unroll
-    for (int r = 0; r < 5; ++r) t[r] += __ldcg(a.part + 5 * q + r);
+    for (int r = 0; r < 5; ++r) csum_add(t[r], tc[r], __ldcg(a.part + 5 * q + r));
   }
-  block_sum<NT, 5>(t, red, tid);
+  block_csum<NT, 5>(t, tc, red, tid);
   if (tid == 0) {
     DevScalars* sc = a.sc;
     sc->E = t[0];

@@ -92,6 +92,12 @@ class Field:
         return L.check(rc, self.h)
 
     # -- state ------------------------------------------------------------
+    def set_state_device(self, om2_ptr: int):
+        """om2 from device memory: a C-contiguous (N, N/2) array of the handle's
+        complex type at om2_ptr (fnm1 = 0, velocity from the om2 inversion)."""
+        self.gen += 1
+        self._ck(self.lib.pal_set_spectral_state(self.h, L.ctypes.c_void_p(int(om2_ptr)), None))
+
     def set_state(self, om2, fnm1=None, uc_low=None):
         self.gen += 1
         om2 = np.ascontiguousarray(om2, dtype=self.cdt)

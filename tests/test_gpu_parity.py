@@ -540,3 +540,31 @@ def test_tma_column_pass_equals_per_lane_column_pass(ts):
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
     F.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_diagnostic_sums_are_compensated_fp64(ts, prec):
+    """The diagnostic sums run in FP64 with compensated (TwoSum) accumulation in
+    both precisions: on the FP32 form's own field (N=1024, 20 RK3 steps) the GPU's
+    E, Z, P and mean(u^2 + v^2) equal the FP64 oracle's sums over the same values
+    -- the downloaded om2 and physical planes, which the diagnostics kernels read
+    -- to 1e-10 relative (turbo_simulator.py:764-810, turbo_main.py:2015-2073)."""
+    from palinstrophy_gb300 import _lib as L
+    N = 1024
+    om2, uc, st = L.pao_generate(N, 15.0, 1e4, 4895, "KM3")
+    F = ts.Field(N, prec, 1e4, 0.1)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", st["visc"])
+    _gpu_init_dt(F)
+    F.step("LS_IMEX_RK3", 20, update=10, final_update=True)
+    d = F.diagnostics()
+    om, u, v = F.om2(), F.ur(0), F.ur(1)
+    S = do.OracleState(N, om.astype(np.complex128), np.zeros((2, N, N // 2), np.complex128), st["visc"], 0.1)
+    S.ur_full[0] = u.astype(np.float64)
+    S.ur_full[1] = v.astype(np.float64)
+    U, _, _ = do.flow_eddy_metrics(S)
+    sp = do.spectral_sums(S)
+    assert abs(d["U"] ** 2 / U ** 2 - 1.0) <= 1e-10
+    for k in ("E", "Z", "P"):
+        assert abs(d[k] / sp[k] - 1.0) <= 1e-10, (k, d[k], sp[k])
+    F.close()

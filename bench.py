@@ -157,18 +157,22 @@ def _limiter(kernel, prec):
             f"FP32 FMA pipe {fma} (profiles/{kernel}_{prec}_N{N_GRID}.md)")
 
 
-def _fp64_flops(kernel):
-    """FP64 flops per launch (2 x DFMA + DADD + DMUL thread instructions) of the
-    FP64 plain path's kernel at N=4096, from the committed ncu summary."""
+def _fp64_counts(kernel, cand):
+    """(FP64 flops, FP64 pipe instructions) per launch of the FP64 plain path's
+    kernel candidate `cand` at N=4096, from the committed ncu summary: flops =
+    2 DFMA + DADD + DMUL thread instructions, pipe instructions = their sum."""
     path = os.path.join(ROOT, "profiles", f"kernels_fp64_N{N_GRID}.md")
+    out = {}
     try:
         with open(path) as f:
             for line in f:
-                if line.strip().startswith(f"fp64_flops_per_launch_{kernel}:"):
-                    return float(line.split(":", 1)[1].split()[0])
+                for key in ("flops", "pipe_inst"):
+                    tag = f"fp64_{key}_per_launch_{kernel}[{cand}]:"
+                    if line.strip().startswith(tag):
+                        out[key] = float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
-    return None
+    return out.get("flops"), out.get("pipe_inst")
 
 
 def _fp64_roofline(om2, uc, visc):
@@ -187,15 +191,21 @@ def _fp64_roofline(om2, uc, visc):
     out = {"bound": "fp64", "unit": "TFLOP/s", "peak": peak,
            "peak_kind": f"measured: FP64 FMA-chain microbenchmark (pal_fp64_peak, {peak_ms:.1f} ms launch)",
            "kernels": desc}
+    cands = {"k_row": desc.split("row[")[1].split("]")[0], "k_col": desc.split("col[")[1].split("]")[0]}
     for name, ms, nbytes in (("k_row", ms_row, 6.0 * n2 * 8), ("k_col", ms_col, (25.0 / 3.0) * n2 * 8)):
-        fl = _fp64_flops(name)
+        fl, inst = _fp64_counts(name, cands[name])
         ach = fl / (ms / 1000.0) / 1e12 if fl else None
-        out[name] = {"ms": ms, "flops_per_launch": fl, "achieved": ach, "frac": ach / peak if ach else None,
+        # the FP64 pipe takes one instruction per slot whether DFMA (2 flops) or
+        # DADD / DMUL (1 flop): the pipe fraction is the FFT's real ceiling
+        pipe = inst / (ms / 1000.0) / (peak * 1e12 / 2.0) if inst else None
+        out[name] = {"ms": ms, "candidate": cands[name], "flops_per_launch": fl, "achieved": ach,
+                     "frac": ach / peak if ach else None, "pipe_inst_per_launch": inst, "pipe_frac": pipe,
                      "hbm_GBps": nbytes / (ms / 1000.0) / 1e9, "hbm_frac": nbytes / (ms / 1000.0) / 1e9 / hbm}
     dom = "k_row" if ms_row >= ms_col else "k_col"
     out["kernel"] = dom
     out["achieved"] = out[dom]["achieved"]
     out["frac"] = out[dom]["frac"]
+    out["pipe_frac"] = out[dom]["pipe_frac"]
     return out
 
 

@@ -7,10 +7,7 @@
 // (LS-IMEX-RK3) regardless of the member count.  Each member keeps its own
 // DevScalars: the fused CFL statistics in the row pass update that member's
 // dt, cn from its own CFLM, so per-member adaptive dt costs no extra launch.
-// The groups share nothing, so each group's launch sequence goes to a stream
-// of its own, forked from and joined back to the ensemble's stream: the groups'
-// kernels run concurrently, and a captured step sequence is a CUDA graph of
-// one independent branch per group.
+// A sequence of steps can be captured once as a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -70,9 +67,6 @@ struct pal_ensemble {
   int precision = 0;
   size_t esz = 8;
   cudaStream_t stream = nullptr;
-  std::vector<cudaStream_t> gstream;  // one per group, for the step sequences
-  std::vector<cudaEvent_t> gdone;     // join events, one per group
-  cudaEvent_t fork = nullptr;
   std::vector<Group> groups;
   std::vector<std::pair<int, int>> where;  // member -> (group, local)
   std::vector<DevScalars> host_sc;
@@ -128,52 +122,54 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
 }
 
 // om / fnm1 of every group into butterfly-major order (to_perm) or back.
-int om_layout(pal_ensemble* e, Group& g, bool to_perm, cudaStream_t s) {
-  StepArgs a = group_args(e, g);
-  if (to_perm)
-    g.ck->to_perm(a, s);
-  else
-    g.ck->from_perm(a, s);
+int om_layout(pal_ensemble* e, bool to_perm) {
+  for (Group& g : e->groups) {
+    StepArgs a = group_args(e, g);
+    if (to_perm)
+      g.ck->to_perm(a, e->stream);
+    else
+      g.ck->from_perm(a, e->stream);
+  }
   cudaError_t c = cudaGetLastError();
   if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble om order: ") + cudaGetErrorString(c));
   return PAL_OK;
 }
 
-// One step of one group; the column pass works on the butterfly-major om / fnm1.
-int launch_step(pal_ensemble* e, Group& g, int method, bool dt_update, cudaStream_t st) {
+// One step of every group; the column pass works on the butterfly-major om / fnm1.
+int launch_step(pal_ensemble* e, int method, bool dt_update) {
   const int stages = method == PAL_CNAB2 ? 1 : 3;
   for (int s = 0; s < stages; ++s) {
-    StepArgs a = group_args(e, g);
-    a.flags = (s == 0 && dt_update) ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
-    g.rk->row(a, st);
-    a = group_args(e, g);
-    a.tw = g.tw_col;
-    a.scheme = method == PAL_CNAB2 ? 0 : 1;
-    if (method != PAL_CNAB2) {
-      a.alpha = kRkAlpha[s];
-      a.beta = kRkBeta[s];
+    for (Group& g : e->groups) {
+      StepArgs a = group_args(e, g);
+      a.flags = (s == 0 && dt_update) ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
+      g.rk->row(a, e->stream);
     }
-    a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
-    if (method != PAL_CNAB2) pal::rk3_stage_flags(a, s, kRkBeta);
-    g.ck->col_perm(a, st);
+    for (Group& g : e->groups) {
+      StepArgs a = group_args(e, g);
+      a.tw = g.tw_col;
+      a.scheme = method == PAL_CNAB2 ? 0 : 1;
+      if (method != PAL_CNAB2) {
+        a.alpha = kRkAlpha[s];
+        a.beta = kRkBeta[s];
+      }
+      a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
+      if (method != PAL_CNAB2) pal::rk3_stage_flags(a, s, kRkBeta);
+      g.ck->col_perm(a, e->stream);
+    }
   }
   cudaError_t c = cudaGetLastError();
   if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble step launch: ") + cudaGetErrorString(c));
   return PAL_OK;
 }
 
-int launch_stats(pal_ensemble* e, Group& g, int flags, cudaStream_t s) {
-  StepArgs a = group_args(e, g);
-  a.flags = flags | pal::F_STATS;
-  g.rk->phys(a, s);
+int launch_stats(pal_ensemble* e, int flags) {
+  for (Group& g : e->groups) {
+    StepArgs a = group_args(e, g);
+    a.flags = flags | pal::F_STATS;
+    g.rk->phys(a, e->stream);
+  }
   cudaError_t c = cudaGetLastError();
   if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble stats: ") + cudaGetErrorString(c));
-  return PAL_OK;
-}
-
-int launch_stats(pal_ensemble* e, int flags) {
-  for (Group& g : e->groups)
-    if (int rc = launch_stats(e, g, flags, e->stream)) return rc;
   return PAL_OK;
 }
 
@@ -271,14 +267,6 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
     }
     if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble setup"));
   }
-  e->gstream.assign(e->groups.size(), nullptr);
-  e->gdone.assign(e->groups.size(), nullptr);
-  c = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
-  for (size_t gi = 0; gi < e->groups.size() && c == cudaSuccess; ++gi) {
-    c = cudaStreamCreateWithFlags(&e->gstream[gi], cudaStreamNonBlocking);
-    if (c == cudaSuccess) c = cudaEventCreateWithFlags(&e->gdone[gi], cudaEventDisableTiming);
-  }
-  if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble group streams"));
   c = cudaStreamSynchronize(e->stream);
   if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_CUDA, "ensemble setup sync"));
   e->host_sc.resize(n_members);
@@ -289,19 +277,12 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
 int pal_ensemble_destroy(pal_ensemble* e) {
   if (!e) return PAL_OK;
   if (e->stream) cudaStreamSynchronize(e->stream);
-  for (cudaStream_t gs : e->gstream)
-    if (gs) cudaStreamSynchronize(gs);
   for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
   for (Group& g : e->groups) {
     void* bufs[] = {g.w0, g.w1, g.om, g.fnm1, g.vel, g.tw_row, g.tw_col, g.phys, g.sc, g.part, g.om_p};
     for (void* b : bufs)
       if (b) cudaFree(b);
   }
-  for (cudaStream_t gs : e->gstream)
-    if (gs) cudaStreamDestroy(gs);
-  for (cudaEvent_t ev : e->gdone)
-    if (ev) cudaEventDestroy(ev);
-  if (e->fork) cudaEventDestroy(e->fork);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return PAL_OK;
@@ -496,22 +477,13 @@ int pal_ensemble_step(pal_ensemble* e, int method, int nsteps, int update, int u
   }
   upd[nsteps] = pending;
   for (bool b : upd) key += b ? '1' : '0';
-  // each group's whole sequence on its own stream, forked from and joined to e->stream
   auto record = [&]() -> int {
-    ENS_CK(e, cudaEventRecord(e->fork, e->stream));
-    for (size_t gi = 0; gi < e->groups.size(); ++gi) {
-      Group& g = e->groups[gi];
-      cudaStream_t gs = e->gstream[gi];
-      ENS_CK(e, cudaStreamWaitEvent(gs, e->fork, 0));
-      if (int rc = om_layout(e, g, true, gs)) return rc;
-      for (int j = 0; j < nsteps; ++j)
-        if (int rc = launch_step(e, g, method, upd[j], gs)) return rc;
-      if (int rc = om_layout(e, g, false, gs)) return rc;
-      if (upd[nsteps])
-        if (int rc = launch_stats(e, g, pal::F_UPDATE_DT, gs)) return rc;
-      ENS_CK(e, cudaEventRecord(e->gdone[gi], gs));
-      ENS_CK(e, cudaStreamWaitEvent(e->stream, e->gdone[gi], 0));
-    }
+    if (int rc = om_layout(e, true)) return rc;
+    for (int j = 0; j < nsteps; ++j)
+      if (int rc = launch_step(e, method, upd[j])) return rc;
+    if (int rc = om_layout(e, false)) return rc;
+    if (upd[nsteps])
+      if (int rc = launch_stats(e, pal::F_UPDATE_DT)) return rc;
     return PAL_OK;
   };
   if (!use_graph) {

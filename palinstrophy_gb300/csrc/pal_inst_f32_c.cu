@@ -41,8 +41,7 @@ const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
                             ColOf<float, RecT<P6144>, 256, 3>::make("16.16.24t x256 hoist pipe0"),
                             ColOf<float, RecT<P6144d>, 256, 3>::make("16.24.16t x256 hoist pipe0"),
                             ColOf<float, Rec<P6144>, 256, 4>::make("16.16.24r x256 tma"),
-                            ColOf<float, Rec<P6144c>, 256, 4>::make("24.16.16r x256 tma"),
-                            ColOf<float, Rec<P6144d>, 256, 4>::make("16.24.16r x256 tma")};
+                            ColOf<float, Rec<P6144>, 256, 8>::make("16.16.24r x256 tma dual")};
 
 PAL_KERNEL_SET(float, 0, 4096, r4096, c4096)
 }  // namespace

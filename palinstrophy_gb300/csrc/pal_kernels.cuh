@@ -1256,21 +1256,100 @@ __device__ __forceinline__ void col_pass_planar(cplx<T>* sm, const cplx<T>* __re
     for (int k = 0; k < R; ++k) p[k * SP] = x[k];
   }
 }
-// DIF passes P .. TO-1, DIT passes P down to TO, each followed by a barrier.
-template <typename T, class PL, int NT, int SIGN, int P, int TO>
-__device__ __forceinline__ void col_dif_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
-  if constexpr (P < TO) {
-    col_pass_planar<T, PL, NT, P, SIGN, false>(sm, tw, tid);
-    __syncthreads();
-    col_dif_planar<T, PL, NT, SIGN, P + 1, TO>(sm, tw, tid);
+// col_pass_planar with a thread's butterflies taken two at a time: both are
+// loaded before either is transformed, so the two DFTs and twiddle products
+// interleave (the compiler cannot move a later butterfly's shared-memory loads
+// above an earlier one's stores, which may alias as far as it can tell).  Same
+// arithmetic per butterfly, so the same results bit for bit.
+template <typename T, class PL, int NT, int P, int SIGN, bool DIT>
+__device__ __forceinline__ void col_pass_planar_dual(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  using C = cplx<T>;
+  using CP = ColPlanar<PL>;
+  constexpr int R = PL::R[P];
+  constexpr int L = PL::span(P);
+  constexpr int S = L / R;
+  constexpr int SP = CP::pstride(P);
+  constexpr int NB = 2 * (PL::M / R);
+  static_assert((PL::M / R) % 16 == 0 && NT % 32 == 0, "whole half-warps per plane");
+  static_assert(S == 1 || S % CP::RP == 0, "strides other than the last are whole pad groups");
+  static_assert(NB % NT == 0, "whole rounds of butterflies");
+  constexpr int ROUNDS = NB / NT;
+  auto place = [&](int w, int& i) -> C* {
+    const int v = (w >> 4) & 1;
+    const int b = ((w >> 5) << 4) | (w & 15);
+    const int blk = b / S;
+    i = b - blk * S;
+    return sm + v * CP::PB + CP::phys(blk * L + i);
+  };
+#pragma unroll
+  for (int r = 0; r + 1 < ROUNDS; r += 2) {
+    int i1, i2;
+    C* p1 = place(tid + r * NT, i1);
+    C* p2 = place(tid + (r + 1) * NT, i2);
+    C x[R], y[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = p1[k * SP];
+#pragma unroll
+    for (int k = 0; k < R; ++k) y[k] = p2[k * SP];
+    if constexpr (DIT) {
+      if constexpr (S > 1) {
+        pass_tw<PL, P, SIGN>(x, tw, i1);
+        pass_tw<PL, P, SIGN>(y, tw, i2);
+      }
+      Dft<R, SIGN, C>::run(x);
+      Dft<R, SIGN, C>::run(y);
+    } else {
+      Dft<R, SIGN, C>::run(x);
+      Dft<R, SIGN, C>::run(y);
+      if constexpr (S > 1) {
+        pass_tw<PL, P, SIGN>(x, tw, i1);
+        pass_tw<PL, P, SIGN>(y, tw, i2);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) p1[k * SP] = x[k];
+#pragma unroll
+    for (int k = 0; k < R; ++k) p2[k * SP] = y[k];
+  }
+  if constexpr (ROUNDS % 2 == 1) {
+    int i;
+    C* p = place(tid + (ROUNDS - 1) * NT, i);
+    C x[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) x[k] = p[k * SP];
+    if constexpr (DIT) {
+      if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
+      Dft<R, SIGN, C>::run(x);
+    } else {
+      Dft<R, SIGN, C>::run(x);
+      if constexpr (S > 1) pass_tw<PL, P, SIGN>(x, tw, i);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) p[k * SP] = x[k];
   }
 }
-template <typename T, class PL, int NT, int SIGN, int P, int TO>
+
+// DIF passes P .. TO-1, DIT passes P down to TO, each followed by a barrier.
+template <typename T, class PL, int NT, int SIGN, int P, int TO, bool DUAL = false>
+__device__ __forceinline__ void col_dif_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
+  if constexpr (P < TO) {
+    if constexpr (DUAL)
+      col_pass_planar_dual<T, PL, NT, P, SIGN, false>(sm, tw, tid);
+    else
+      col_pass_planar<T, PL, NT, P, SIGN, false>(sm, tw, tid);
+    __syncthreads();
+    col_dif_planar<T, PL, NT, SIGN, P + 1, TO, DUAL>(sm, tw, tid);
+  }
+}
+template <typename T, class PL, int NT, int SIGN, int P, int TO, bool DUAL = false>
 __device__ __forceinline__ void col_dit_planar(cplx<T>* sm, const cplx<T>* __restrict__ tw, int tid) {
   if constexpr (P >= TO) {
-    col_pass_planar<T, PL, NT, P, SIGN, true>(sm, tw, tid);
+    if constexpr (DUAL)
+      col_pass_planar_dual<T, PL, NT, P, SIGN, true>(sm, tw, tid);
+    else
+      col_pass_planar<T, PL, NT, P, SIGN, true>(sm, tw, tid);
     __syncthreads();
-    col_dit_planar<T, PL, NT, SIGN, P - 1, TO>(sm, tw, tid);
+    col_dit_planar<T, PL, NT, SIGN, P - 1, TO, DUAL>(sm, tw, tid);
   }
 }
 
@@ -1282,8 +1361,10 @@ __device__ __forceinline__ void col_dit_planar(cplx<T>* sm, const cplx<T>* __res
 // by bulk tensor stores that skip the pads.  om / fnm1 are the butterfly-major
 // columns (om_p, fm_p), read and written by the lanes as in k_col.  Same
 // arithmetic as k_col, so the same results bit for bit.  FP32.
-// MINB > 0 caps the registers so that MINB blocks share an SM.
-template <typename T, class PL, int NT, bool QM, int MINB = 0>
+// MINB > 0 caps the registers so that MINB blocks share an SM.  DUAL: the
+// passes around the middle take a thread's butterflies two at a time
+// (col_pass_planar_dual).
+template <typename T, class PL, int NT, bool QM, int MINB = 0, bool DUAL = false>
 __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = cplx<T>;
   using CP = ColPlanar<PL>;
@@ -1317,9 +1398,9 @@ __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_
     if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
     mbar_test_wait(&bar, 0, 1 << 20);
   }
-  col_dif_planar<T, PL, NT, -1, 0, PL::NP - 1>(sm, tw, tid);
+  col_dif_planar<T, PL, NT, -1, 0, PL::NP - 1, DUAL>(sm, tw, tid);
   col_middle<T, PL, NT, false, true, true, QM, true>(sm, nullptr, nullptr, om, fm, cf, kx, tid, a.flags);
-  col_dit_planar<T, PL, NT, +1, PL::NP - 2, 0>(sm, tw, tid);
+  col_dit_planar<T, PL, NT, +1, PL::NP - 2, 0, DUAL>(sm, tw, tid);
   fence_proxy_async_smem();
   __syncthreads();
   if (tid == 0) {

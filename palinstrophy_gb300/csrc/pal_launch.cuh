@@ -161,7 +161,10 @@ struct ColOf {
   // PREF 4: the butterfly-major pass is k_col_tma (planar tile, TMA bulk
   // copies of the planes); the natural-order pass is the plain k_col.
   // PREF 5 / 6: the same with registers capped for three / two blocks per SM.
-  static constexpr bool TMA = PREF == 4 || PREF == 5 || PREF == 6;
+  // PREF 8: PREF 4 with the passes around the middle taking two butterflies
+  // per thread at a time.
+  static constexpr bool TMA = PREF == 4 || PREF == 5 || PREF == 6 || PREF == 8;
+  static constexpr bool DUAL = PREF == 8;
   static constexpr int BASE = TMA ? 0 : PREF;
   static constexpr size_t smem_inv = size_t(PL::PADM) * 2 * sizeof(cplx<T>);
   static constexpr size_t smem = smem_inv + (BASE == 1 ? size_t(2) * (2 * PL::M / 3) * sizeof(cplx<T>) : 0);
@@ -176,14 +179,14 @@ struct ColOf {
         cudaFuncSetAttribute(k_col<T, PL, NT, BASE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if constexpr (TMA) {
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB, DUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB, DUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_tma);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, true, MINB, DUAL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      e = cudaFuncSetAttribute(k_col_tma<T, PL, NT, false, MINB, DUAL>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
     }
@@ -216,9 +219,9 @@ struct ColOf {
       static const TmaMaps none{};
       const TmaMaps& m = a.cmaps ? *a.cmaps : none;
       if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
-        k_col_tma<T, PL, NT, true, MINB><<<grid(a), NT, smem_tma, s>>>(a, m);
+        k_col_tma<T, PL, NT, true, MINB, DUAL><<<grid(a), NT, smem_tma, s>>>(a, m);
       else
-        k_col_tma<T, PL, NT, false, MINB><<<grid(a), NT, smem_tma, s>>>(a, m);
+        k_col_tma<T, PL, NT, false, MINB, DUAL><<<grid(a), NT, smem_tma, s>>>(a, m);
       return;
     }
     if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
@@ -241,7 +244,7 @@ struct ColOf {
     int n = 0;
     cudaError_t e;
     if constexpr (TMA)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col_tma<T, PL, NT, false, MINB>, NT, smem_tma);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col_tma<T, PL, NT, false, MINB, DUAL>, NT, smem_tma);
     else
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_col<T, PL, NT, PERM_PREF, true, false>, NT, smem_inv);
     return e == cudaSuccess ? n : -1;

@@ -289,36 +289,46 @@ def _e2e(prec, om2, uc, visc, steps):
 def _ensemble_rate(steps=1000, warmup=20):
     """Batched ensemble: 96 members (32 each at N=256, 384, 512), seeds 1-96, KM3
     K0=10, Re=1e4, CNAB2, per-member adaptive dt at CFL 0.5 (NEXTDT every step,
-    fused into the row pass), FP32, replayed from a CUDA graph."""
+    fused into the row pass), FP32, replayed from a CUDA graph.  Default: one
+    launch per pass for all three sizes (2 per CNAB2 step); for comparison the
+    per-size launches (6 per step) of candidates re-tuned on each group's
+    batched shape."""
     import torch
     from palinstrophy_gb300 import _lib as L
     from palinstrophy_gb300.turbo_simulator import Ensemble
     Ns = [256] * 32 + [384] * 32 + [512] * 32
-    E = Ensemble(Ns, "fp32", 1e4, 0.5)
-    E.autotune()  # candidates timed on the batched launch shape of each size group
-    for m, n in enumerate(Ns):
-        om2, uc, st = L.pao_generate(n, 10.0, 1e4, m + 1, "KM3")
-        E.set_member(m, om2, None, uc)
-        E.set_scalar(m, "visc", st["visc"])
-    E.init_dt()
-    s = torch.cuda.ExternalStream(E.stream_ptr())
-    E.step("CNAB2", warmup, update=1, graph=True)
-    E.step("CNAB2", steps, update=1, graph=True)  # capture
-    E.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    E.step("CNAB2", steps, update=1, graph=True)
-    e1.record(s)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    dts = sorted(E.scalars(m)["dt"] for m in (0, 40, 95))
-    variants = {n: E.variant(n) for n in (256, 384, 512)}
-    E.close()
-    return {"members": len(Ns), "sizes": [256, 384, 512], "steps": steps,
-            "ensemble_steps_per_s": steps / (ms / 1000.0),
-            "member_steps_per_s": len(Ns) * steps / (ms / 1000.0),
-            "launches_per_step": 6, "cuda_graph": True, "sample_member_dt": dts, "kernels": variants}
+    inits = [L.pao_generate(n, 10.0, 1e4, m + 1, "KM3") for m, n in enumerate(Ns)]
+    out = {}
+    for mode in ("fused", "per_size_tuned"):
+        E = Ensemble(Ns, "fp32", 1e4, 0.5)
+        if mode == "per_size_tuned":
+            E.autotune()  # candidates timed on the batched launch shape of each size group
+        for m, (om2, uc, st) in enumerate(inits):
+            E.set_member(m, om2, None, uc)
+            E.set_scalar(m, "visc", st["visc"])
+        E.init_dt()
+        s = torch.cuda.ExternalStream(E.stream_ptr())
+        E.step("CNAB2", warmup, update=1, graph=True)
+        E.step("CNAB2", steps, update=1, graph=True)  # capture
+        E.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        E.step("CNAB2", steps, update=1, graph=True)
+        e1.record(s)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[mode] = {"ensemble_steps_per_s": steps / (ms / 1000.0),
+                     "member_steps_per_s": len(Ns) * steps / (ms / 1000.0),
+                     "launches_per_step": 2 if mode == "fused" else 6,
+                     "kernels": {n: E.variant(n) for n in (256, 384, 512)},
+                     "sample_member_dt": sorted(E.scalars(m)["dt"] for m in (0, 40, 95))}
+        E.close()
+    f = out["fused"]
+    return {"members": len(Ns), "sizes": [256, 384, 512], "steps": steps, "cuda_graph": True,
+            "ensemble_steps_per_s": f["ensemble_steps_per_s"], "member_steps_per_s": f["member_steps_per_s"],
+            "launches_per_step": 2, "one_launch_per_pass": True, "kernels": f["kernels"],
+            "sample_member_dt": f["sample_member_dt"], "per_size_tuned": out["per_size_tuned"]}
 
 
 def _differentiation(directions=8):

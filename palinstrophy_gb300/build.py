@@ -26,7 +26,7 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I" + INCLUDE]
 
 CU_SOURCES = ["pal_inst_f32_a.cu", "pal_inst_f32_e.cu", "pal_inst_f32_f.cu", "pal_inst_f32_b.cu", "pal_inst_f32_c.cu", "pal_inst_f32_d.cu",
               "pal_inst_f64_a.cu", "pal_inst_f64_b.cu", "pal_inst.cu", "pal_api.cu", "pal_noalloc.cu", "pal_measure.cu",
-              "pal_ensemble.cu", "pal_generate.cu"]
+              "pal_ensemble.cu", "pal_ens_fused.cu", "pal_generate.cu"]
 CPP_SOURCES = ["pal_pao.cpp"]
 
 

@@ -7,6 +7,11 @@
 // (LS-IMEX-RK3) regardless of the member count.  Each member keeps its own
 // DevScalars: the fused CFL statistics in the row pass update that member's
 // dt, cn from its own CFLM, so per-member adaptive dt costs no extra launch.
+// When every group's size belongs to a compiled fused set (pal_ens_fused.cu,
+// FP32), each pass is instead ONE launch over all groups -- 2 launches per
+// CNAB2 step, 6 per LS-IMEX-RK3 step, whatever the number of sizes -- with the
+// set's fixed candidates; pal_ensemble_autotune switches to per-size launches
+// of candidates re-tuned on each group's batched shape.
 // A sequence of steps can be captured once as a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
@@ -46,6 +51,7 @@ struct Group {
   DevScalars* sc = nullptr;
   double* part = nullptr;
   long long part_stride = 0;
+  int slot = -1;  // size index in the fused set, when the ensemble runs fused passes
 };
 
 // dt = cflnum / (CFLM pi), cn = 1, cnm1 = 0, t = 0, it = 0 for every member of a group
@@ -71,6 +77,7 @@ struct pal_ensemble {
   std::vector<std::pair<int, int>> where;  // member -> (group, local)
   std::vector<DevScalars> host_sc;
   std::map<std::string, cudaGraphExec_t> graphs;
+  const pal::FusedSet* fused = nullptr;  // one launch per pass over all groups, or per-size launches
   long long it = 0;
   bool ready = false;  // velocities resolved, dt initialised
   bool has_members = false;  // a member has been set (the buffers hold state)
@@ -122,7 +129,34 @@ StepArgs group_args(const pal_ensemble* e, const Group& g) {
 }
 
 // om / fnm1 of every group into butterfly-major order (to_perm) or back.
+// The group table of a fused pass: `per_member(g)` blocks per member of group g.
+template <class PerMember, class ArgsOf>
+int fused_args(const pal_ensemble* e, pal::FusedArgs& f, PerMember per_member, ArgsOf args_of) {
+  std::memset(&f, 0, sizeof(f));
+  f.ngroups = (int)e->groups.size();
+  int blocks = 0;
+  for (int gi = 0; gi < f.ngroups; ++gi) {
+    const Group& g = e->groups[gi];
+    f.g[gi].a = args_of(g);
+    f.g[gi].slot = g.slot;
+    f.g[gi].first = blocks;
+    f.g[gi].per_member = per_member(g);
+    f.maps[gi] = g.tmaps;
+    blocks += f.g[gi].per_member * (int)g.members.size();
+  }
+  return blocks;
+}
+
 int om_layout(pal_ensemble* e, bool to_perm) {
+  if (e->fused) {
+    pal::FusedArgs f;
+    const int nb = fused_args(e, f, [](const Group& g) { return g.Nh; },
+                              [&](const Group& g) { return group_args(e, g); });
+    (to_perm ? e->fused->to_perm : e->fused->from_perm)(f, nb, e->stream);
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble om order: ") + cudaGetErrorString(c));
+    return PAL_OK;
+  }
   for (Group& g : e->groups) {
     StepArgs a = group_args(e, g);
     if (to_perm)
@@ -139,12 +173,12 @@ int om_layout(pal_ensemble* e, bool to_perm) {
 int launch_step(pal_ensemble* e, int method, bool dt_update) {
   const int stages = method == PAL_CNAB2 ? 1 : 3;
   for (int s = 0; s < stages; ++s) {
-    for (Group& g : e->groups) {
+    auto row_args = [&](const Group& g) {
       StepArgs a = group_args(e, g);
       a.flags = (s == 0 && dt_update) ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
-      g.rk->row(a, e->stream);
-    }
-    for (Group& g : e->groups) {
+      return a;
+    };
+    auto col_args = [&](const Group& g) {
       StepArgs a = group_args(e, g);
       a.tw = g.tw_col;
       a.scheme = method == PAL_CNAB2 ? 0 : 1;
@@ -154,8 +188,18 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
       }
       a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
       if (method != PAL_CNAB2) pal::rk3_stage_flags(a, s, kRkBeta);
-      g.ck->col_perm(a, e->stream);
+      return a;
+    };
+    if (e->fused) {
+      pal::FusedArgs f;
+      int nb = fused_args(e, f, [](const Group& g) { return g.M / g.rk->V; }, row_args);
+      e->fused->row(f, nb, e->stream);
+      nb = fused_args(e, f, [](const Group& g) { return g.Nh; }, col_args);
+      e->fused->col(f, nb, e->stream);
+      continue;
     }
+    for (Group& g : e->groups) g.rk->row(row_args(g), e->stream);
+    for (Group& g : e->groups) g.ck->col_perm(col_args(g), e->stream);
   }
   cudaError_t c = cudaGetLastError();
   if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble step launch: ") + cudaGetErrorString(c));
@@ -163,6 +207,18 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
 }
 
 int launch_stats(pal_ensemble* e, int flags) {
+  if (e->fused) {
+    pal::FusedArgs f;
+    const int nb = fused_args(e, f, [](const Group& g) { return g.M / g.rk->V; }, [&](const Group& g) {
+      StepArgs a = group_args(e, g);
+      a.flags = flags | pal::F_STATS;
+      return a;
+    });
+    e->fused->phys(f, nb, e->stream);
+    cudaError_t c = cudaGetLastError();
+    if (c != cudaSuccess) return efail(e, PAL_ERR_CUDA, std::string("ensemble stats: ") + cudaGetErrorString(c));
+    return PAL_OK;
+  }
   for (Group& g : e->groups) {
     StepArgs a = group_args(e, g);
     a.flags = flags | pal::F_STATS;
@@ -217,15 +273,38 @@ int pal_ensemble_create(int n_members, const int* N, int precision, double Re, d
   }
   cudaError_t c = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (c != cudaSuccess) return bail(efail(nullptr, PAL_ERR_CUDA, "cudaStreamCreate"));
+  // one launch per pass when a fused set holds every size (PAL_ENSEMBLE_FUSED=0: per-size launches)
+  {
+    const char* fenv = std::getenv("PAL_ENSEMBLE_FUSED");
+    std::vector<int> gN;
+    for (const Group& g : e->groups) gN.push_back(g.N);
+    if (precision == PAL_FP32 && !(fenv && fenv[0] == '0'))
+      e->fused = pal_fused_set_f32((int)gN.size(), gN.data());
+    for (Group& g : e->groups) {
+      if (!e->fused) break;
+      const pal::FusedSet* fs = e->fused;
+      g.slot = (int)(std::find(fs->N, fs->N + fs->nsizes, g.N) - fs->N);
+      for (int q = 0; q < g.ks->n_rows; ++q)
+        if (std::strcmp(g.ks->rows[q].name, fs->row_name[g.slot]) == 0) g.rk = &g.ks->rows[q];
+      for (int q = 0; q < g.ks->n_cols; ++q)
+        if (std::strcmp(g.ks->cols[q].name, fs->col_name[g.slot]) == 0) g.ck = &g.ks->cols[q];
+      if (!g.rk || !g.ck || g.rk->V != fs->V[g.slot]) e->fused = nullptr;  // candidates not compiled: per-size
+    }
+    if (e->fused && e->fused->configure() != cudaSuccess) e->fused = nullptr;
+    if (!e->fused)
+      for (Group& g : e->groups) g.rk = nullptr, g.ck = nullptr, g.slot = -1;
+  }
   for (Group& g : e->groups) {
-    // the autotuned candidates of this size (tuned once per process by pal_create)
-    pal_handle* tmp = nullptr;
-    if (int rc = pal_create(g.N, precision, Re, cfl, &tmp)) return bail(efail(nullptr, rc, "autotune probe failed"));
-    int r = 0, cc = 0;
-    pal_get_variant(tmp, &r, &cc, nullptr, nullptr, nullptr, 0);
-    pal_destroy(tmp);
-    g.rk = &g.ks->rows[r];
-    g.ck = &g.ks->cols[cc];
+    if (!e->fused) {
+      // the autotuned candidates of this size (tuned once per process by pal_create)
+      pal_handle* tmp = nullptr;
+      if (int rc = pal_create(g.N, precision, Re, cfl, &tmp)) return bail(efail(nullptr, rc, "autotune probe failed"));
+      int r = 0, cc = 0;
+      pal_get_variant(tmp, &r, &cc, nullptr, nullptr, nullptr, 0);
+      pal_destroy(tmp);
+      g.rk = &g.ks->rows[r];
+      g.ck = &g.ks->cols[cc];
+    }
     const size_t nm = g.members.size();
     const size_t plane_w = (size_t)g.Nh * g.M * e->esz, plane_om = (size_t)g.Nh * g.N * e->esz;
     g.part_stride = std::max<long long>(2LL * g.M, 5 * 1024);
@@ -326,6 +405,8 @@ int pal_ensemble_autotune(pal_ensemble* e) {
   if (e->has_members) return efail(e, PAL_ERR_STATE, "autotune before setting members");
   const char* env = std::getenv("PAL_AUTOTUNE");
   if (env && env[0] == '0') return PAL_OK;
+  e->fused = nullptr;  // re-tuned candidates run as per-size launches
+  for (Group& g : e->groups) g.slot = -1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   ENS_CK(e, cudaEventCreate(&e0));
   ENS_CK(e, cudaEventCreate(&e1));
@@ -407,7 +488,7 @@ int pal_ensemble_get_variant(pal_ensemble* e, int group_N, char* desc, size_t de
   if (!e || !desc || !desc_len) return efail(e, PAL_ERR_INVALID, "bad arguments");
   for (const Group& g : e->groups) {
     if (g.N == group_N) {
-      std::snprintf(desc, desc_len, "row[%s] col[%s]", g.rk->name, g.ck->name);
+      std::snprintf(desc, desc_len, "%srow[%s] col[%s]", e->fused ? "fused " : "", g.rk->name, g.ck->name);
       return PAL_OK;
     }
   }

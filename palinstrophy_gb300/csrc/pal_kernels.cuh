@@ -105,9 +105,17 @@ struct TmaMaps {  // aligned as CUtensorMap
   CUtensorMap w0, w1;
 };
 
-// Member view of the arguments for block row blockIdx.y.
-__device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz) {
-  const long long m = blockIdx.y;
+// A block's place in its pass: x = tile or column index within the member,
+// y = member, nx = blocks per member (the count the last-block reductions wait
+// for).  A kernel launched for one group takes it from blockIdx / gridDim
+// (hw_blk); the ensemble's one-launch passes decode it from a block table.
+struct Blk {
+  int x, y, nx;
+};
+__device__ __forceinline__ Blk hw_blk() { return Blk{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x}; }
+
+// Member view of the arguments for member m.
+__device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz, long long m) {
   if (m == 0) return a;
   StepArgs b = a;
   b.w0 = static_cast<char*>(a.w0) + m * a.ms_w * esz;
@@ -121,6 +129,10 @@ __device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz) {
   b.sc = a.sc + m;
   b.part = a.part + m * a.ms_part;
   return b;
+}
+// ... for block row blockIdx.y.
+__device__ __forceinline__ StepArgs member_args(const StepArgs& a, size_t esz) {
+  return member_args(a, esz, (long long)blockIdx.y);
 }
 
 constexpr double kPi = 3.14159265358979323846;
@@ -222,17 +234,22 @@ __device__ __forceinline__ void block_csum(double (&s)[K], double (&c)[K], doubl
   __syncthreads();
 }
 
-// Returns true in every thread of the block that finished last.
-__device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
+// Returns true in every thread of the block that finished last of the nx
+// blocks counting on `counter`.
+__device__ __forceinline__ bool last_block(unsigned int* counter, int tid, int nx) {
   __shared__ int is_last;
   __threadfence();
   __syncthreads();
   if (tid == 0) {
     const unsigned int ticket = atomicAdd(counter, 1u);
-    is_last = (ticket == gridDim.x - 1u);  // blocks of this member (grid row)
+    is_last = (ticket == (unsigned)nx - 1u);
   }
   __syncthreads();
   return is_last != 0;
+}
+// ... of the blocks of this member (grid row).
+__device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
+  return last_block(counter, tid, (int)gridDim.x);
 }
 
 // Physical-space statistics of one block: (max |u|+|v|, sum u^2+v^2) -> partials;
@@ -240,18 +257,18 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
 // sum arrives as a thread's compensated pair (sum, comp) and stays compensated
 // through the block tree and the reduction of the partials.
 template <int NT>
-__device__ void finish_stats(const StepArgs& a, double mx, double sum, double comp, int M, int tid) {
+__device__ void finish_stats(const StepArgs& a, double mx, double sum, double comp, int M, int tid, const Blk& bk) {
   __shared__ double red[2 * (NT / 32)];
   mx = block_max<NT>(mx, red, tid);
   double s1[1] = {sum}, c1[1] = {comp};
   block_csum<NT, 1>(s1, c1, red, tid);
   if (tid == 0) {
-    a.part[2 * blockIdx.x] = mx;
-    a.part[2 * blockIdx.x + 1] = s1[0];
+    a.part[2 * bk.x] = mx;
+    a.part[2 * bk.x + 1] = s1[0];
   }
-  const bool last = last_block(&a.sc->row_counter, tid);
+  const bool last = last_block(&a.sc->row_counter, tid, bk.nx);
   if (!last) return;
-  const int nb = gridDim.x;
+  const int nb = bk.nx;
   double m2 = 0.0, s2[1] = {0.0}, c2[1] = {0.0};
   for (int q = tid; q < nb; q += NT) {
     m2 = fmax(m2, __ldcg(a.part + 2 * q));
@@ -468,7 +485,7 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
 // No thread spends load instructions or LSU queue entries on global memory.
 template <typename T, class PL, int V, int NT>
 __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* sm, int z0, int tid,
-                                                   const TmaMaps& maps, unsigned long long* bar) {
+                                                   const TmaMaps& maps, unsigned long long* bar, int member) {
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int R = PL::R[0];
@@ -486,8 +503,8 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
     mbar_expect_tx(bar, 2u * Nh * V * (unsigned)sizeof(C));
 #pragma unroll 1
     for (int bx = 0; bx < Nh / BOX; ++bx) {
-      tma_load_3d(&maps.w0, sm + (size_t)bx * BOX * V, bar, 2 * z0, bx * BOX, (int)blockIdx.y);
-      tma_load_3d(&maps.w1, sm + (size_t)(Nh + bx * BOX) * V, bar, 2 * z0, bx * BOX, (int)blockIdx.y);
+      tma_load_3d(&maps.w0, sm + (size_t)bx * BOX * V, bar, 2 * z0, bx * BOX, member);
+      tma_load_3d(&maps.w1, sm + (size_t)(Nh + bx * BOX) * V, bar, 2 * z0, bx * BOX, member);
     }
   }
   if (!mbar_wait(bar, 0, a.dbg_wait0 ? 0 : 1 << 22)) {
@@ -622,7 +639,7 @@ __device__ __forceinline__ void row_last_pass_paired(const StepArgs& a, cplx<T>*
 // the plane writes and they drain while the next tile starts.
 template <typename T, class PL, int V, int NT>
 __device__ __forceinline__ void row_last_pass_tma(const StepArgs& a, cplx<T>* sm, int z0, int tid,
-                                                  const TmaMaps& maps) {
+                                                  const TmaMaps& maps, int member) {
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int R = PL::R[0];
@@ -686,8 +703,8 @@ __device__ __forceinline__ void row_last_pass_tma(const StepArgs& a, cplx<T>* sm
   if (tid == 0) {
 #pragma unroll 1
     for (int bx = 0; bx < Nh / BOX; ++bx) {
-      tma_store_3d(&maps.w0, stg + (size_t)bx * BOX * V, 2 * z0, bx * BOX, (int)blockIdx.y);
-      tma_store_3d(&maps.w1, stg + (size_t)(Nh + bx * BOX) * V, 2 * z0, bx * BOX, (int)blockIdx.y);
+      tma_store_3d(&maps.w0, stg + (size_t)bx * BOX * V, 2 * z0, bx * BOX, member);
+      tma_store_3d(&maps.w1, stg + (size_t)(Nh + bx * BOX) * V, 2 * z0, bx * BOX, member);
     }
     tma_commit();
     tma_wait_read();  // the shared memory stays the block's until the engine has read it
@@ -721,20 +738,19 @@ constexpr int row_tiles_per_sm() {
   return int(size_t(228 * 1024) / (size_t(PL::PADM) * V * sizeof(cplx<T>) + 1024 + 256));
 }
 template <typename T, class PL, int V, int NT, int PF>
-__global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() : 0)
-    k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
+__device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps, const Blk bk) {
   using C = cplx<T>;
-  const StepArgs a = member_args(a0, sizeof(C));
+  const StepArgs a = member_args(a0, sizeof(C), bk.y);
   extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   const int tid = threadIdx.x;
-  const int z0 = blockIdx.x * V;
+  const int z0 = bk.x * V;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
 
   if constexpr ((PF & 1) != 0) {
-    const int nb = (int)blockIdx.x + a.ahead;
-    if (a.ahead > 0 && nb < (int)gridDim.x) {
+    const int nb = bk.x + a.ahead;
+    if (a.ahead > 0 && nb < bk.nx) {
       constexpr int Nh = M / 3;
       const cplx<T>* w0 = static_cast<const cplx<T>*>(a.w0) + (size_t)nb * V;
       const cplx<T>* w1 = static_cast<const cplx<T>*>(a.w1) + (size_t)nb * V;
@@ -745,7 +761,7 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
     __shared__ __align__(8) unsigned long long tma_bar;
     if (tid == 0) mbar_init(&tma_bar, 1);
     __syncthreads();
-    row_first_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, &tma_bar);
+    row_first_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, &tma_bar, bk.y);
   } else if constexpr ((PF & 2) != 0) {
     row_first_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
   } else {
@@ -793,7 +809,7 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
   if constexpr (sizeof(C) == 8) {
     dit_range<T, PL, V, NT, -1, PL::NP - 2, 1>(sm, tw, tid);
     if constexpr ((PF & 4) != 0)
-      row_last_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps);
+      row_last_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, bk.y);
     else
       row_last_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
   } else {
@@ -811,19 +827,24 @@ __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() :
       w1[(size_t)k * M + z0 + v] = C{T(0.5) * (p.y + q.y), T(-0.5) * (p.x - q.x)};
     }
   }
-  if (stats) finish_stats<NT>(a, double(mx), acc, comp, M, tid);
+  if (stats) finish_stats<NT>(a, double(mx), acc, comp, M, tid, bk);
+}
+template <typename T, class PL, int V, int NT, int PF>
+__global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() : 0)
+    k_row(StepArgs a0, const __grid_constant__ TmaMaps maps) {
+  row_body<T, PL, V, NT, PF>(a0, maps, hw_blk());
 }
 
 // k_phys: U-state rows -> physical u, v (statistics, optional plane store).
 template <typename T, class PL, int V, int NT>
-__global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
+__device__ __forceinline__ void phys_body(const StepArgs& a0, const Blk bk) {
   using C = cplx<T>;
-  const StepArgs a = member_args(a0, sizeof(C));
+  const StepArgs a = member_args(a0, sizeof(C), bk.y);
   extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   const int tid = threadIdx.x;
-  const int z0 = blockIdx.x * V;
+  const int z0 = bk.x * V;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
   dif_range<T, PL, V, NT, +1, 1, PL::NP>(sm, tw, tid);
@@ -844,7 +865,11 @@ __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
       ph[(size_t)M * M + (size_t)(z0 + v) * M + n] = val.y;
     }
   }
-  finish_stats<NT>(a, double(mx), acc, comp, M, tid);
+  finish_stats<NT>(a, double(mx), acc, comp, M, tid, bk);
+}
+template <typename T, class PL, int V, int NT>
+__global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {
+  phys_body<T, PL, V, NT>(a0, hw_blk());
 }
 
 // --------------------------------------------------------------------------
@@ -1107,9 +1132,9 @@ __device__ __forceinline__ void col_last_pass(const cplx<T>* sm, cplx<T>* __rest
 
 // Time / cnm1 bookkeeping of the step, done once by the last block to finish.
 template <int NT>
-__device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
+__device__ __forceinline__ void col_finish(const StepArgs& a, int tid, int nx) {
   if (a.flags & (F_ADVANCE | F_CNM1)) {
-    if (last_block(&a.sc->col_counter, tid) && tid == 0) {
+    if (last_block(&a.sc->col_counter, tid, nx) && tid == 0) {
       DevScalars* sc = a.sc;
       if (a.flags & F_ADVANCE) {
         sc->t += sc->dt;
@@ -1129,15 +1154,15 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid) {
 // PERM the kernel works on om_p / fm_p (butterfly-major columns of M elements).
 // QM: the RK3 stage flags F_Q_IN / F_Q_OUT / F_NO_FM_IN are honoured (col_middle).
 template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true>
-__global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
+__device__ __forceinline__ void col_body(const StepArgs& a0, const Blk bk) {
   using C = cplx<T>;
-  const StepArgs a = member_args(a0, sizeof(C));
+  const StepArgs a = member_args(a0, sizeof(C), bk.y);
   extern __shared__ __align__(128) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   constexpr int M = PL::M;
   constexpr int V = 2;
   const int tid = threadIdx.x;
-  const int kx = blockIdx.x;
+  const int kx = bk.x;
   constexpr int N = 2 * M / 3;
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   C* __restrict__ w0 = static_cast<C*>(a.w0);
@@ -1218,7 +1243,11 @@ __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
                                                                              tid, a.flags);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
-  col_finish<NT>(a, tid);
+  col_finish<NT>(a, tid, bk.nx);
+}
+template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true>
+__global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
+  col_body<T, PL, NT, PREF, PERM, QM>(a0, hw_blk());
 }
 
 // One DIF (DIT = false) or DIT pass over a planar column tile (ColPlanar):
@@ -1412,7 +1441,7 @@ __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_
     tma_commit();
     tma_wait_read();  // the shared memory stays the block's until the engine has read it
   }
-  col_finish<NT>(a, tid);
+  col_finish<NT>(a, tid, (int)gridDim.x);
 }
 
 // om / fnm1 between the natural [kx][z] columns and the butterfly-major
@@ -1420,28 +1449,28 @@ __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_
 // M-element column are written or read).  One block per kx column; the column
 // passes through shared memory, so both the natural and the butterfly-major
 // side are read and written in consecutive order.
-template <typename T, class PL, bool TO_PERM>
-__global__ void __launch_bounds__(256) k_om_perm(StepArgs a0) {
+template <typename T, class PL, bool TO_PERM, int NT>
+__device__ __forceinline__ void om_perm_body(const StepArgs& a0, const Blk bk) {
   using C = cplx<T>;
-  const StepArgs a = member_args(a0, sizeof(C));
+  const StepArgs a = member_args(a0, sizeof(C), bk.y);
   constexpr int M = PL::M, N = 2 * M / 3, Nh = M / 3;
   constexpr int RP = PL::RP, FSTEP = PL::FSTEP;
   extern __shared__ __align__(128) unsigned char smraw[];
   C* so = reinterpret_cast<C*>(smraw);
   C* sf = so + N;
-  const int kx = blockIdx.x;
+  const int kx = bk.x;
   C* __restrict__ no = static_cast<C*>(a.om) + (size_t)kx * N;
   C* __restrict__ nf = static_cast<C*>(a.fnm1) + (size_t)kx * N;
   C* __restrict__ po = static_cast<C*>(a.om_p) + (size_t)kx * M;
   C* __restrict__ pf = static_cast<C*>(a.fm_p) + (size_t)kx * M;
   if constexpr (TO_PERM) {
-    for (int z = threadIdx.x; z < N; z += 256) {
+    for (int z = threadIdx.x; z < N; z += NT) {
       so[z] = no[z];
       sf[z] = nf[z];
     }
     __syncthreads();
   }
-  for (int p = threadIdx.x; p < M; p += 256) {
+  for (int p = threadIdx.x; p < M; p += NT) {
     const int f = PL::freq((p % FSTEP) * RP) + (p / FSTEP) * FSTEP;
     if (f < Nh || f >= N) {
       const int z = f < Nh ? f : f - Nh;
@@ -1456,11 +1485,15 @@ __global__ void __launch_bounds__(256) k_om_perm(StepArgs a0) {
   }
   if constexpr (!TO_PERM) {
     __syncthreads();
-    for (int z = threadIdx.x; z < N; z += 256) {
+    for (int z = threadIdx.x; z < N; z += NT) {
       no[z] = so[z];
       nf[z] = sf[z];
     }
   }
+}
+template <typename T, class PL, bool TO_PERM>
+__global__ void __launch_bounds__(256) k_om_perm(StepArgs a0) {
+  om_perm_body<T, PL, TO_PERM, 256>(a0, hw_blk());
 }
 
 // k_col_inv: velocity low band -> pad -> inverse z-FFT -> U planes.  The low

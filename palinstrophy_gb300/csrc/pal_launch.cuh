@@ -110,7 +110,7 @@ inline int wave_blocks(K kernel, int nt, size_t smem) {
 // fnm1: the first stage reads no fnm1, the first two hand the next stage its
 // combined q in om (k_col F_Q_OUT / F_Q_IN), the last stores om and fn.
 // `beta` is the stage table of beta coefficients.
-inline void rk3_stage_flags(StepArgs& a, int s, const double* beta) {
+__host__ __device__ inline void rk3_stage_flags(StepArgs& a, int s, const double* beta) {
   a.flags |= (s == 0 ? F_NO_FM_IN : F_Q_IN) | (s < 2 ? F_Q_OUT : 0);
   a.beta_next = s < 2 ? beta[s + 1] : 0.0;
 }
@@ -337,7 +337,43 @@ void launch_pixels(const void* plane, long long n, double* part, unsigned int* c
                                            ::pal::launch_pixels<T>,                                     \
                                            ADJ};
 
+// One launch per pass for an ensemble of several sizes (pal_ens_fused.cu).  The
+// blocks of a pass are laid out group by group, member by member: group g's
+// blocks start at `first`, `per_member` of them per member; every block
+// decodes its (group, member, index) and runs that size's kernel body.
+constexpr int kFusedMax = 4;
+struct FusedGroupArgs {
+  StepArgs a;      // the group's arguments (all of its members)
+  int slot;        // which compiled size of the fused set this group is
+  int first;       // first block of the group in the launch
+  int per_member;  // blocks per member in this pass
+};
+struct FusedArgs {  // aligned as CUtensorMap
+  TmaMaps maps[kFusedMax];  // row-tile TMA descriptors of each group
+  FusedGroupArgs g[kFusedMax];
+  int ngroups;
+};
+// A compiled set of sizes with fixed kernel candidates of one block size.
+struct FusedSet {
+  int nsizes;
+  int N[kFusedMax];
+  const char* row_name[kFusedMax];  // the KernelSet candidates whose twiddle tables
+  const char* col_name[kFusedMax];  // and TMA layout the fused bodies share
+  int V[kFusedMax];                 // row tile height of each size
+  int NT;
+  size_t smem_row, smem_col, smem_perm;
+  cudaError_t (*configure)();
+  void (*row)(const FusedArgs&, int blocks, cudaStream_t);
+  void (*col)(const FusedArgs&, int blocks, cudaStream_t);
+  void (*phys)(const FusedArgs&, int blocks, cudaStream_t);
+  void (*to_perm)(const FusedArgs&, int blocks, cudaStream_t);
+  void (*from_perm)(const FusedArgs&, int blocks, cudaStream_t);
+};
+
 }  // namespace pal
+
+// The fused set holding every size in Ns (FP32), or nullptr.
+const pal::FusedSet* pal_fused_set_f32(int n, const int* Ns);
 
 // Per-precision lookup (pal_inst_f32.cu / pal_inst_f64.cu); nullptr if unsupported.
 const pal::KernelSet* pal_kernels_f32(int N);

@@ -185,3 +185,76 @@ def test_members_with_bulk_tensor_row_loads(ts):
         assert np.array_equal(F.fnm1(), E.fnm1(m)), m
         F.close()
     E.close()
+
+
+def _force(F, desc):
+    """Select the row / column candidates named in an ensemble variant string."""
+    want_row = desc.split("row[")[1].split("]")[0]
+    want_col = desc.split("col[")[1].split("]")[0]
+    v = F.variant()
+    r = c = None
+    for i in range(v["n_rows"]):
+        F.set_variant(i, 0)
+        if F.variant()["desc"].split("row[")[1].split("]")[0] == want_row:
+            r = i
+    for j in range(v["n_cols"]):
+        F.set_variant(0, j)
+        if F.variant()["desc"].split("col[")[1].split("]")[0] == want_col:
+            c = j
+    assert r is not None and c is not None, desc
+    F.set_variant(r, c)
+
+
+@pytest.mark.parametrize("method", ["CNAB2", "LS_IMEX_RK3"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_fused_passes_over_three_sizes(ts, method, graph):
+    """Members of N = 256, 384 and 512 advance with ONE launch per pass for all
+    sizes (the groups' blocks laid out in one grid, each block running its
+    size's kernel body); every member equals the same field stepped alone with
+    the same kernel candidates, bit for bit, with its own adaptive dt."""
+    Ns = [256, 384, 512, 256, 512, 384]
+    seeds = [1, 2, 3, 4, 5, 6]
+    E = ts.Ensemble(Ns, "fp32", 1e4, 0.5)
+    for n in (256, 384, 512):
+        assert E.variant(n).startswith("fused row[")
+    for m, (n, sd) in enumerate(zip(Ns, seeds)):
+        om2, uc, st = _member_init(n, sd)
+        E.set_member(m, om2, None, uc)
+        E.set_scalar(m, "visc", st["visc"])
+    E.init_dt()
+    E.step(method, 5, update=2, graph=graph)
+    E.step(method, 5, update=2, graph=graph)
+    E.synchronize()
+    dts = []
+    for m, (n, sd) in enumerate(zip(Ns, seeds)):
+        om2, uc, st = _member_init(n, sd)
+        F = ts.Field(n, "fp32", 1e4, 0.5)
+        _force(F, E.variant(n))
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.step2a()
+        F.set_scalar("dt", 0.5 / (F.compute_cflm() * math.pi))
+        F.set_scalar("cn", 1.0)
+        F.set_scalar("cnm1", 0.0)
+        F.set_scalar("it", 0)
+        F.step(method, 10, update=2)
+        assert np.array_equal(F.om2(), E.om2(m)), m
+        assert np.array_equal(F.fnm1(), E.fnm1(m)), m
+        se, sf = E.scalars(m), F.scalars()
+        assert se["dt"] == sf["dt"] and se["it"] == 10
+        dts.append(se["dt"])
+        F.close()
+    assert len(set(dts)) > 1
+    E.close()
+
+
+def test_fused_passes_off_and_after_autotune(ts, monkeypatch):
+    """PAL_ENSEMBLE_FUSED=0 and a batched re-tune both give per-size launches."""
+    E = ts.Ensemble([256, 384], "fp32", 1e4, 0.5)
+    E.autotune()
+    assert not E.variant(256).startswith("fused")
+    E.close()
+    monkeypatch.setenv("PAL_ENSEMBLE_FUSED", "0")
+    E = ts.Ensemble([256, 384], "fp32", 1e4, 0.5)
+    assert not E.variant(384).startswith("fused")
+    E.close()

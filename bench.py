@@ -261,6 +261,12 @@ def _e2e(prec, om2, uc, visc, steps):
     h_out = pin_out.numpy().view(cdt).reshape(om2.shape)
     h_om[...] = om2
     h_uc[...] = uc
+    # one untimed pass through the same pinned buffers: the first DMA from
+    # freshly pinned pages can take 10-20 ms more, a one-off cost of the buffers
+    W = Field(N_GRID, prec, RE, CFL)
+    W.set_state(h_om, None, h_uc)
+    W._ck(W.lib.pal_get_field(W.h, 0, h_out.ctypes.data_as(__import__("ctypes").c_void_p)))
+    W.close()
     F = Field(N_GRID, prec, RE, CFL)
     F.synchronize()
     t0 = time.perf_counter()

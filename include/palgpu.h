@@ -206,10 +206,13 @@ int pal_step_noalloc(int N, int method, int nsteps, double dt, double visc, doub
 
 /* Batched ensembles (the reference runs one field per process; this is the
  * GB300 form for many independent fields): members with their own N, seed,
- * viscosity, CFL target and adaptive dt advance together, one launch per
- * group of equal N per pass (grid.y = members), optionally replayed from a
- * CUDA graph.  No counterpart in the reference API; each member follows the
- * single-field semantics of pal_step. */
+ * viscosity, CFL target and adaptive dt advance together, optionally replayed
+ * from a CUDA graph.  When every member's N belongs to a compiled fused set
+ * (FP32: N = 256, 384, 512) each pass is ONE launch over all members of all
+ * sizes (2 launches per CNAB2 step, 6 per LS-IMEX-RK3 step); otherwise, or
+ * with PAL_ENSEMBLE_FUSED=0 in the environment, one launch per group of equal
+ * N per pass (grid.y = members).  No counterpart in the reference API; each
+ * member follows the single-field semantics of pal_step. */
 typedef struct pal_ensemble pal_ensemble;
 int pal_ensemble_create(int n_members, const int* N, int precision, double Re, double cfl, pal_ensemble** out);
 int pal_ensemble_destroy(pal_ensemble* e);
@@ -225,10 +228,11 @@ int pal_ensemble_init_dt(pal_ensemble* e);
  * it % update == 0 or it == 1 (update > 0); use_graph captures the launch
  * sequence once per pattern and replays it. */
 int pal_ensemble_step(pal_ensemble* e, int method, int nsteps, int update, int use_graph);
-/* Re-tune each group's row / column candidates on its batched launch shape;
- * call right after pal_ensemble_create, before any member is set.  Without it
- * the groups use the single-field choice of pal_create (members then match
- * single fields bit for bit; tuned groups match them to rounding). */
+/* Re-tune each group's row / column candidates on its batched launch shape and
+ * run per-size launches of them; call right after pal_ensemble_create, before
+ * any member is set.  Without it the groups use the fused set's candidates or
+ * the single-field choice of pal_create (members then match single fields of
+ * those candidates bit for bit; tuned groups match them to rounding). */
 int pal_ensemble_autotune(pal_ensemble* e);
 /* Candidates of the group of size group_N, as "row[...] col[...]". */
 int pal_ensemble_get_variant(pal_ensemble* e, int group_N, char* desc, size_t desc_len);

@@ -726,7 +726,7 @@ int pal_next_dt(pal_handle* h, int sync_host, double* cflm) {
 int pal_diagnostics(pal_handle* h, pal_diag* out) {
   if (int rc = check(h)) return rc;
   if (!out) return fail(h, PAL_ERR_INVALID, "out is null");
-  if (int rc = launch_phys(h, 0)) return rc;
+  if (int rc = launch_phys(h, pal::F_DIAG)) return rc;
   StepArgs a = base_args(h);
   h->ks->spectral(a, h->stream, h->spectral_blocks);
   PAL_LAUNCHED(h, "k_spectral");

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "pal_launch.cuh"
 
@@ -32,13 +33,12 @@ struct FusedSize {
   static __device__ __forceinline__ void row(const StepArgs& a, const TmaMaps& m, Blk bk) {
     row_body<float, PLR, VR, NT, PFR>(a, m, bk);
   }
-  template <int NT>
+  // QM: the flag-aware update of the RK3 stages that carry the combined term,
+  // else the plain update (a separate launch, so CNAB2 passes keep the plain
+  // body's register budget), as ColOf::col_perm chooses
+  template <int NT, bool QM>
   static __device__ __forceinline__ void col(const StepArgs& a, Blk bk) {
-    // the flag-aware update (RK3 stages carrying the combined term) as in ColOf::col_perm
-    if (a.flags & (F_Q_IN | F_Q_OUT | F_NO_FM_IN))
-      col_body<float, PLC, NT, PREFC, true, true>(a, bk);
-    else
-      col_body<float, PLC, NT, PREFC, true, false>(a, bk);
+    col_body<float, PLC, NT, PREFC, true, QM>(a, bk);
   }
   template <int NT>
   static __device__ __forceinline__ void phys(const StepArgs& a, Blk bk) {
@@ -63,13 +63,14 @@ __device__ __forceinline__ int fused_place(const FusedArgs& f, Blk& bk) {
   return g;
 }
 
-enum Pass { P_ROW, P_COL, P_PHYS, P_TO, P_FROM };
+enum Pass { P_ROW, P_COL, P_COL_QM, P_PHYS, P_TO, P_FROM };
 
 template <int PASS, int NT, int I, class S0, class... Ss>
 __device__ __forceinline__ void fused_run(int slot, const FusedArgs& f, int g, Blk bk) {
   if (slot == I) {
     if constexpr (PASS == P_ROW) S0::template row<NT>(f.g[g].a, f.maps[g], bk);
-    if constexpr (PASS == P_COL) S0::template col<NT>(f.g[g].a, bk);
+    if constexpr (PASS == P_COL) S0::template col<NT, false>(f.g[g].a, bk);
+    if constexpr (PASS == P_COL_QM) S0::template col<NT, true>(f.g[g].a, bk);
     if constexpr (PASS == P_PHYS) S0::template phys<NT>(f.g[g].a, bk);
     if constexpr (PASS == P_TO) S0::template perm<NT, true>(f.g[g].a, bk);
     if constexpr (PASS == P_FROM) S0::template perm<NT, false>(f.g[g].a, bk);
@@ -85,18 +86,29 @@ __global__ void __launch_bounds__(NT) k_ens_fused(const __grid_constant__ FusedA
   fused_run<PASS, NT, 0, Ss...>(f.g[g].slot, f, g, bk);
 }
 
-template <int NT, class... Ss>
+template <int NT, int NTC, class... Ss>
 struct FusedOf {
   static constexpr size_t smem_row = std::max({Ss::smem_row...});
   static constexpr size_t smem_col = std::max({Ss::smem_col...});
   static constexpr size_t smem_perm = std::max({Ss::smem_perm...});
   static_assert(smem_row <= kSmemLimit && smem_col <= kSmemLimit, "fused tiles fit in shared memory");
+  // row and statistics passes run NT threads per block, the column and layout
+  // passes NTC
+  template <int PASS>
+  static constexpr int threads() {
+    return (PASS == P_ROW || PASS == P_PHYS) ? NT : NTC;
+  }
   template <int PASS>
   static void launch(const FusedArgs& f, int blocks, size_t smem, cudaStream_t s) {
-    k_ens_fused<PASS, NT, Ss...><<<blocks, NT, smem, s>>>(f);
+    k_ens_fused<PASS, threads<PASS>(), Ss...><<<blocks, threads<PASS>(), smem, s>>>(f);
   }
   static void row(const FusedArgs& f, int blocks, cudaStream_t s) { launch<P_ROW>(f, blocks, smem_row, s); }
-  static void col(const FusedArgs& f, int blocks, cudaStream_t s) { launch<P_COL>(f, blocks, smem_col, s); }
+  static void col(const FusedArgs& f, int blocks, bool qm, cudaStream_t s) {
+    if (qm)
+      launch<P_COL_QM>(f, blocks, smem_col, s);
+    else
+      launch<P_COL>(f, blocks, smem_col, s);
+  }
   static void phys(const FusedArgs& f, int blocks, cudaStream_t s) { launch<P_PHYS>(f, blocks, smem_row, s); }
   static void to_perm(const FusedArgs& f, int blocks, cudaStream_t s) { launch<P_TO>(f, blocks, smem_perm, s); }
   static void from_perm(const FusedArgs& f, int blocks, cudaStream_t s) { launch<P_FROM>(f, blocks, smem_perm, s); }
@@ -105,10 +117,11 @@ struct FusedOf {
       const void* k;
       size_t smem;
     } ks[] = {{(const void*)k_ens_fused<P_ROW, NT, Ss...>, smem_row},
-              {(const void*)k_ens_fused<P_COL, NT, Ss...>, smem_col},
+              {(const void*)k_ens_fused<P_COL, NTC, Ss...>, smem_col},
+              {(const void*)k_ens_fused<P_COL_QM, NTC, Ss...>, smem_col},
               {(const void*)k_ens_fused<P_PHYS, NT, Ss...>, smem_row},
-              {(const void*)k_ens_fused<P_TO, NT, Ss...>, smem_perm},
-              {(const void*)k_ens_fused<P_FROM, NT, Ss...>, smem_perm}};
+              {(const void*)k_ens_fused<P_TO, NTC, Ss...>, smem_perm},
+              {(const void*)k_ens_fused<P_FROM, NTC, Ss...>, smem_perm}};
     for (const auto& k : ks) {
       cudaError_t e = cudaFuncSetAttribute(k.k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
       if (e != cudaSuccess) return e;
@@ -118,35 +131,55 @@ struct FusedOf {
 };
 
 // The 96-member configuration's sizes: N = 256, 384, 512 (M = 384, 576, 768).
+// One block size for all bodies means one register budget (the largest body's):
+// the light plans are chosen (the 6.6.16 row plan at N=384 needs ~60 registers
+// where the 24.24 plan needs 128).
 using P384 = Plan<384, 16, 24>;
 using P576 = Plan<576, 24, 24>;
+using P576b = Plan<576, 6, 6, 16>;
+using P768 = Plan<768, 32, 24>;
 using P768b = Plan<768, 16, 2, 24>;
 using S256 = FusedSize<Rec<P384>, 4, 14, Rec<P384>, 2>;
-using S384 = FusedSize<Rec<P576>, 4, 14, Rec<P576>, 2>;
-using S512 = FusedSize<Rec<P768b>, 4, 14, Rec<P768b>, 2>;
-using F3 = FusedOf<128, S256, S384, S512>;
+using S384 = FusedSize<Rec<P576b>, 2, 14, Rec<P576>, 2>;
+using S512 = FusedSize<Rec<P768b>, 4, 14, Rec<P768>, 2>;
+using S256p = FusedSize<Rec<P384>, 4, 14, P384, 0>;
 
-const FusedSet kSet3 = {3,
-                        {256, 384, 512},
-                        {"16.24r V4x128 tma-in tma-out", "24.24r V4x128 tma-in tma-out l2pf",
-                         "16.2.24r V4x128 tma-in tma-out"},
-                        {"16.24r x128 hoist", "24.24r x128 hoist", "16.2.24r x128 hoist"},
-                        {4, 4, 4},
-                        128,
-                        F3::smem_row,
-                        F3::smem_col,
-                        F3::smem_perm,
-                        F3::configure,
-                        F3::row,
-                        F3::col,
-                        F3::phys,
-                        F3::to_perm,
-                        F3::from_perm};
+#define PAL_FUSED_SET(NAME, F, COL256)                                                                   \
+  const FusedSet NAME = {3,                                                                              \
+                         {256, 384, 512},                                                                \
+                         {"16.24r V4x128 tma-in tma-out", "6.6.16r V2x128 tma-in tma-out",               \
+                          "16.2.24r V4x128 tma-in tma-out"},                                             \
+                         {COL256, "24.24r x128 hoist", "32.24r x128 hoist"},                             \
+                         {4, 2, 4},                                                                      \
+                         128,                                                                            \
+                         F::smem_row,                                                                    \
+                         F::smem_col,                                                                    \
+                         F::smem_perm,                                                                   \
+                         F::configure,                                                                   \
+                         F::row,                                                                         \
+                         F::col,                                                                         \
+                         F::phys,                                                                        \
+                         F::to_perm,                                                                     \
+                         F::from_perm};
+using FA = FusedOf<128, 128, S256, S384, S512>;
+using FB = FusedOf<128, 64, S256p, S384, S512>;
+using FC = FusedOf<128, 64, S256, S384, S512>;
+PAL_FUSED_SET(kSetA, FA, "16.24r x128 hoist")
+PAL_FUSED_SET(kSetB, FB, "16.24 x64")
+PAL_FUSED_SET(kSetC, FC, "16.24r x128 hoist")
+#undef PAL_FUSED_SET
+const FusedSet* const kSets[] = {&kSetB, &kSetA, &kSetC};
 
 }  // namespace
 
+// PAL_ENSEMBLE_FUSED=k (k >= 1) selects the k-th compiled variant of the set
+// (column block size and candidates); the first is the default.
 const pal::FusedSet* pal_fused_set_f32(int n, const int* Ns) {
+  int k = 1;
+  if (const char* env = std::getenv("PAL_ENSEMBLE_FUSED")) k = std::atoi(env);
+  if (k < 1 || k > (int)(sizeof(kSets) / sizeof(kSets[0])) || n <= 0 || n > kFusedMax) return nullptr;
+  const FusedSet* fs = kSets[k - 1];
   for (int i = 0; i < n; ++i)
-    if (std::find(kSet3.N, kSet3.N + kSet3.nsizes, Ns[i]) == kSet3.N + kSet3.nsizes) return nullptr;
-  return n > 0 && n <= kFusedMax ? &kSet3 : nullptr;
+    if (std::find(fs->N, fs->N + fs->nsizes, Ns[i]) == fs->N + fs->nsizes) return nullptr;
+  return fs;
 }

@@ -195,7 +195,8 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
       int nb = fused_args(e, f, [](const Group& g) { return g.M / g.rk->V; }, row_args);
       e->fused->row(f, nb, e->stream);
       nb = fused_args(e, f, [](const Group& g) { return g.Nh; }, col_args);
-      e->fused->col(f, nb, e->stream);
+      const bool qm = (f.g[0].a.flags & (pal::F_Q_IN | pal::F_Q_OUT | pal::F_NO_FM_IN)) != 0;
+      e->fused->col(f, nb, qm, e->stream);
       continue;
     }
     for (Group& g : e->groups) g.rk->row(row_args(g), e->stream);

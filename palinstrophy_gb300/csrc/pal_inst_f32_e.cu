@@ -19,7 +19,8 @@ const RowKernels r384[] = {RowOf<float, P576, 4, 256>::make("24.24 V4x256"),
                            RowOf<float, Rec<P576>, 4, 128, 15>::make("24.24r V4x128 tma-in tma-out l2pf"),
                            RowOf<float, Rec<P576>, 4, 256, 15>::make("24.24r V4x256 tma-in tma-out l2pf"),
                            RowOf<float, Rec<P576b>, 4, 192, 15>::make("6.6.16r V4x192 tma-in tma-out l2pf"),
-                           RowOf<float, Rec<P576b>, 4, 192, 14>::make("6.6.16r V4x192 tma-in tma-out")};
+                           RowOf<float, Rec<P576b>, 4, 192, 14>::make("6.6.16r V4x192 tma-in tma-out"),
+                           RowOf<float, Rec<P576b>, 2, 128, 14>::make("6.6.16r V2x128 tma-in tma-out")};
 const ColKernels c384[] = {ColOf<float, P576, 128>::make("24.24 x128"), ColOf<float, P576b, 128>::make("6.6.16 x128"),
                            ColOf<float, Rec<P576>, 128, 2>::make("24.24r x128 hoist")};
 const RowKernels r512[] = {RowOf<float, P768, 4, 256>::make("32.24 V4x256"),

@@ -33,6 +33,7 @@ enum : int {
   F_NO_FM_IN = 32,  // the update does not read fnm1 (its weight c3 is 0: first stage)
   F_Q_IN = 64,      // om holds q = (1 - K2 h1) om + c3 fnm1 of this stage; fnm1 is not read
   F_Q_OUT = 128,    // write the next stage's q (weights from beta_next) into om, not om and fn
+  F_DIAG = 256,     // k_phys: the diagnostic sum of u^2+v^2, compensated FP64 (else a plain sum)
 };
 
 // Device-resident scalars, FP64 in both precisions.
@@ -253,15 +254,21 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
 }
 
 // Physical-space statistics of one block: (max |u|+|v|, sum u^2+v^2) -> partials;
-// the last block reduces all partials in a fixed order and applies NEXTDT.  The
-// sum arrives as a thread's compensated pair (sum, comp) and stays compensated
-// through the block tree and the reduction of the partials.
-template <int NT>
+// the last block reduces all partials in a fixed order and applies NEXTDT.  With
+// COMP the sum arrives as a thread's compensated pair (sum, comp) and stays
+// compensated through the block tree and the reduction of the partials (the
+// diagnostic sum); without it the sum is a plain FP64 tree, enough for the
+// finiteness check of the NEXTDT statistics and far cheaper in FP64 issue slots,
+// which matters for small tiles that take the statistics every step.
+template <int NT, bool COMP>
 __device__ void finish_stats(const StepArgs& a, double mx, double sum, double comp, int M, int tid, const Blk& bk) {
   __shared__ double red[2 * (NT / 32)];
   mx = block_max<NT>(mx, red, tid);
   double s1[1] = {sum}, c1[1] = {comp};
-  block_csum<NT, 1>(s1, c1, red, tid);
+  if constexpr (COMP)
+    block_csum<NT, 1>(s1, c1, red, tid);
+  else
+    block_sum<NT, 1>(s1, red, tid);
   if (tid == 0) {
     a.part[2 * bk.x] = mx;
     a.part[2 * bk.x + 1] = s1[0];
@@ -272,10 +279,16 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, double co
   double m2 = 0.0, s2[1] = {0.0}, c2[1] = {0.0};
   for (int q = tid; q < nb; q += NT) {
     m2 = fmax(m2, __ldcg(a.part + 2 * q));
-    csum_add(s2[0], c2[0], __ldcg(a.part + 2 * q + 1));
+    if constexpr (COMP)
+      csum_add(s2[0], c2[0], __ldcg(a.part + 2 * q + 1));
+    else
+      s2[0] += __ldcg(a.part + 2 * q + 1);
   }
   m2 = block_max<NT>(m2, red, tid);
-  block_csum<NT, 1>(s2, c2, red, tid);
+  if constexpr (COMP)
+    block_csum<NT, 1>(s2, c2, red, tid);
+  else
+    block_sum<NT, 1>(s2, red, tid);
   if (tid == 0) {
     DevScalars* sc = a.sc;
     const double cflm = m2 * (double(a.N) / (2.0 * kPi));
@@ -770,9 +783,12 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
   dif_range<T, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
 
   // middle: last inverse DIF pass -> products -> first forward DIT pass
+  // NEXTDT needs the CFL maximum; the sum of u^2 + v^2 here only serves the
+  // finiteness check (a NaN drops out of a max), so it is a plain sum in the
+  // working precision.  The diagnostic mean(u^2 + v^2) is k_phys's compensated
+  // FP64 sum (pal_diagnostics).
   const bool stats = (a.flags & F_STATS) != 0;
-  T mx = T(0);
-  double acc = 0.0, comp = 0.0;  // compensated FP64 sum of u^2 + v^2
+  T mx = T(0), acc = T(0);
   {
     constexpr int R = PL::RP;
     constexpr int NB = V * (M / R);
@@ -785,15 +801,12 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
       for (int j = 0; j < R; ++j) x[j] = p[j * V];
       Dft<R, +1, C>::run(x);
       if (stats) {
-        double b = 0.0;  // this butterfly's R points, squares in FP64
 #pragma unroll
         for (int j = 0; j < R; ++j) {
           const T u = x[j].x, q = x[j].y;
           mx = fmax(mx, fabs(u) + fabs(q));
-          const double du = double(u), dq = double(q);
-          b = fma(du, du, fma(dq, dq, b));
+          acc = fma(u, u, fma(q, q, acc));
         }
-        csum_add(acc, comp, b);
       }
 #pragma unroll
       for (int j = 0; j < R; ++j) {
@@ -827,7 +840,7 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
       w1[(size_t)k * M + z0 + v] = C{T(0.5) * (p.y + q.y), T(-0.5) * (p.x - q.x)};
     }
   }
-  if (stats) finish_stats<NT>(a, double(mx), acc, comp, M, tid, bk);
+  if (stats) finish_stats<NT, false>(a, double(mx), double(acc), 0.0, M, tid, bk);
 }
 template <typename T, class PL, int V, int NT, int PF>
 __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() : 0)
@@ -848,24 +861,32 @@ __device__ __forceinline__ void phys_body(const StepArgs& a0, const Blk bk) {
   const C* __restrict__ tw = static_cast<const C*>(a.tw);
   row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
   dif_range<T, PL, V, NT, +1, 1, PL::NP>(sm, tw, tid);
-  T mx = T(0);
-  double acc = 0.0, comp = 0.0;  // compensated FP64 sum of u^2 + v^2
+  T mx = T(0), accp = T(0);
+  double acc = 0.0, comp = 0.0;  // F_DIAG: compensated FP64 sum of u^2 + v^2
   T* __restrict__ ph = static_cast<T*>(a.phys);
   const bool store = (a.flags & F_PHYS) != 0;
+  const bool diag = (a.flags & F_DIAG) != 0;
   for (int w = tid; w < V * M; w += NT) {
     const int v = w % V;
     const int pos = w / V;
     const C val = sm[PL::phys(pos) * V + v];
     mx = fmax(mx, fabs(val.x) + fabs(val.y));
-    const double du = double(val.x), dq = double(val.y);
-    csum_add(acc, comp, fma(du, du, dq * dq));
+    if (diag) {
+      const double du = double(val.x), dq = double(val.y);
+      csum_add(acc, comp, fma(du, du, dq * dq));
+    } else {
+      accp = fma(val.x, val.x, fma(val.y, val.y, accp));  // finiteness check only
+    }
     if (store) {
       const int n = PL::freq(pos);
       ph[(size_t)(z0 + v) * M + n] = val.x;
       ph[(size_t)M * M + (size_t)(z0 + v) * M + n] = val.y;
     }
   }
-  finish_stats<NT>(a, double(mx), acc, comp, M, tid, bk);
+  if (diag)
+    finish_stats<NT, true>(a, double(mx), acc, comp, M, tid, bk);
+  else
+    finish_stats<NT, false>(a, double(mx), double(accp), 0.0, M, tid, bk);
 }
 template <typename T, class PL, int V, int NT>
 __global__ void __launch_bounds__(NT) k_phys(StepArgs a0) {

@@ -364,7 +364,7 @@ struct FusedSet {
   size_t smem_row, smem_col, smem_perm;
   cudaError_t (*configure)();
   void (*row)(const FusedArgs&, int blocks, cudaStream_t);
-  void (*col)(const FusedArgs&, int blocks, cudaStream_t);
+  void (*col)(const FusedArgs&, int blocks, bool qm, cudaStream_t);  // qm: RK3 stages (ColOf::col_perm)
   void (*phys)(const FusedArgs&, int blocks, cudaStream_t);
   void (*to_perm)(const FusedArgs&, int blocks, cudaStream_t);
   void (*from_perm)(const FusedArgs&, int blocks, cudaStream_t);

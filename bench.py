@@ -680,6 +680,7 @@ def run_gb300(args):
     # FP32 form: headline
     F = _field("fp32", om2, uc, visc)
     ms_row, ms_col, _ = F.profile_kernels(METHOD, 3)
+    kernels32 = F.variant()["desc"]
     F.close()
     F = _field("fp32", om2, uc, visc)
     ms32, clocks = _timed_steps(F, args.steps, args.warmup, sampler_index=local)
@@ -760,7 +761,7 @@ def run_gb300(args):
         # timed region = one pal_step call: 6 launches per RK3 step, the two om/fnm1
         # order conversions, and a k_phys launch if the last step ends on the NEXTDT cadence
         "gpu_launches": 6 * args.steps + 2 + int((args.warmup + args.steps) % UPDATE == 0),
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": dominant, "kernels": kernels32, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(dominant, "fp32"), "algorithmic_bytes": dom_bytes,
                      "ms_per_launch": {"k_row": ms_row, "k_col": ms_col},

@@ -133,7 +133,7 @@ struct RowOf {
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
     }
-    if (PF & 1) ahead = ((PF & 32) ? 2 : 1) * wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
+    if (PF & (1 | 64)) ahead = ((PF & 32) ? 2 : 1) * wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   static void row(const StepArgs& a, cudaStream_t s) {
@@ -357,10 +357,10 @@ struct FusedArgs {  // aligned as CUtensorMap
 struct FusedSet {
   int nsizes;
   int N[kFusedMax];
-  const char* row_name[kFusedMax];  // the KernelSet candidates whose twiddle tables
-  const char* col_name[kFusedMax];  // and TMA layout the fused bodies share
+  const char* row_name[kFusedMax];  // the KernelSet candidates whose twiddle tables (same plan)
+  const char* col_name[kFusedMax];  // and TMA row layout (same tile height) the fused bodies use
   int V[kFusedMax];                 // row tile height of each size
-  int NT;
+  int NT;  // row-pass block size (the column passes may use another)
   size_t smem_row, smem_col, smem_perm;
   cudaError_t (*configure)();
   void (*row)(const FusedArgs&, int blocks, cudaStream_t);

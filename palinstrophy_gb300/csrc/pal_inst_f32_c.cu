@@ -28,8 +28,7 @@ const RowKernels r4096[] = {RowOf<float, P6144, 4, 512>::make("16.16.24 V4x512")
                             RowOf<float, Rec<P6144>, 2, 384, 30>::make("16.16.24r V2x384 tma-in tma-out"),
                             RowOf<float, Rec<P6144c>, 2, 256, 30>::make("24.16.16r V2x256 tma-in tma-out"),
                             RowOf<float, RecT<P6144c>, 2, 256, 30>::make("24.16.16t V2x256 tma-in tma-out"),
-                            RowOf<float, Rec<P6144d>, 2, 384, 30>::make("16.24.16r V2x384 tma-in tma-out"),
-                            RowOf<float, RecT<P6144c>, 2, 256, 94>::make("24.16.16t V2x256 tma-in tma-out tpf")};
+                            RowOf<float, Rec<P6144d>, 2, 384, 30>::make("16.24.16r V2x384 tma-in tma-out")};
 const ColKernels c4096[] = {ColOf<float, P6144, 256>::make("16.16.24 x256"),
                             ColOf<float, Rec<P6144c>, 256>::make("24.16.16r x256"),
                             ColOf<float, Rec<P6144>, 256>::make("16.16.24r x256"),

@@ -15,8 +15,7 @@ const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"
                             RowOf<float, Rec<P12288>, 2, 768, 15>::make("16.32.24r V2x768 tma-in tma-out l2pf"),
                             RowOf<float, Rec<P12288>, 2, 768, 11>::make("16.32.24r V2x768 tma-in l2pf"),
                             RowOf<float, RecT<P12288>, 2, 768, 15>::make("16.32.24t V2x768 tma-in tma-out l2pf"),
-                            RowOf<float, RecT<P12288>, 2, 768, 14>::make("16.32.24t V2x768 tma-in tma-out"),
-                            RowOf<float, RecT<P12288>, 2, 768, 78>::make("16.32.24t V2x768 tma-in tma-out tpf")};
+                            RowOf<float, RecT<P12288>, 2, 768, 14>::make("16.32.24t V2x768 tma-in tma-out")};
 const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
                             ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),

@@ -383,13 +383,6 @@ __device__ __forceinline__ void tma_load_3d(const CUtensorMap* map, void* smem, 
       "l"(map), "r"(b), "r"(x), "r"(y), "r"(z)
       : "memory");
 }
-// Ask the TMA unit to bring a box of a tensor into L2 (no shared memory, no
-// completion to wait for: a hint).
-__device__ __forceinline__ void tma_prefetch_l2_3d(const CUtensorMap* map, int x, int y, int z) {
-  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(map), "r"(x), "r"(y),
-               "r"(z)
-               : "memory");
-}
 // Wait for phase `parity` of the mbarrier with non-blocking polls
 // (mbarrier.test_wait), giving up after max_iter of them: a bound in time even
 // if the expected transaction count were never reached.
@@ -505,8 +498,7 @@ __device__ __forceinline__ void row_first_pass_paired(const StepArgs& a, cplx<T>
 // No thread spends load instructions or LSU queue entries on global memory.
 template <typename T, class PL, int V, int NT>
 __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* sm, int z0, int tid,
-                                                   const TmaMaps& maps, unsigned long long* bar, int member,
-                                                   int z_ahead = -1) {
+                                                   const TmaMaps& maps, unsigned long long* bar, int member) {
   using C = cplx<T>;
   constexpr int M = PL::M;
   constexpr int R = PL::R[0];
@@ -526,13 +518,6 @@ __device__ __forceinline__ void row_first_pass_tma(const StepArgs& a, cplx<T>* s
     for (int bx = 0; bx < Nh / BOX; ++bx) {
       tma_load_3d(&maps.w0, sm + (size_t)bx * BOX * V, bar, 2 * z0, bx * BOX, member);
       tma_load_3d(&maps.w1, sm + (size_t)(Nh + bx * BOX) * V, bar, 2 * z0, bx * BOX, member);
-    }
-    if (z_ahead >= 0) {  // the rows of the tile one wave ahead, into L2
-#pragma unroll 1
-      for (int bx = 0; bx < Nh / BOX; ++bx) {
-        tma_prefetch_l2_3d(&maps.w0, 2 * z_ahead, bx * BOX, member);
-        tma_prefetch_l2_3d(&maps.w1, 2 * z_ahead, bx * BOX, member);
-      }
     }
   }
   if (!mbar_wait(bar, 0, a.dbg_wait0 ? 0 : 1 << 22)) {
@@ -756,9 +741,6 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
 // PF bit 2 (value 4): the last pass stores through the TMA unit (row_last_pass_tma).
 // PF bit 3 (value 8): the first pass loads through the TMA unit (row_first_pass_tma).
 // PF bit 5 (value 32): with bit 0, the prefetched tile is two waves ahead.
-// PF bit 6 (value 64): with TMA loads, the thread that issues them also asks
-// the TMA unit to prefetch the tile one wave ahead into L2 (a few bulk
-// prefetch instructions per tile instead of a line prefetch per row).
 // PF bit 4 (value 16): registers are capped so that as many blocks share an SM
 // as its shared memory holds tiles (row_tiles_per_sm); without it the
 // launch bound names no block count and the compiler chooses.
@@ -792,10 +774,7 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
     __shared__ __align__(8) unsigned long long tma_bar;
     if (tid == 0) mbar_init(&tma_bar, 1);
     __syncthreads();
-    int z_ahead = -1;
-    if constexpr ((PF & 64) != 0)
-      if (a.ahead > 0 && bk.x + a.ahead < bk.nx) z_ahead = (bk.x + a.ahead) * V;
-    row_first_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, &tma_bar, bk.y, z_ahead);
+    row_first_pass_tma<T, PL, V, NT>(a, sm, z0, tid, maps, &tma_bar, bk.y);
   } else if constexpr ((PF & 2) != 0) {
     row_first_pass_paired<T, PL, V, NT>(a, sm, z0, tid);
   } else {

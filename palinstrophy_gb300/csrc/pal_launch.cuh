@@ -133,7 +133,7 @@ struct RowOf {
                                (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return e;
     }
-    if (PF & (1 | 64)) ahead = ((PF & 32) ? 2 : 1) * wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
+    if (PF & 1) ahead = ((PF & 32) ? 2 : 1) * wave_blocks(k_row<T, PL, V, NT, PF>, NT, smem);
     return cudaFuncSetAttribute(k_phys<T, PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   static void row(const StepArgs& a, cudaStream_t s) {

@@ -1,10 +1,12 @@
 // FP32 candidates, N = 8192 (M = 12288).
 #include "pal_launch.cuh"
+#include "pal_row_split.cuh"
 
 using namespace pal;
 
 namespace {
 using P12288 = Plan<12288, 16, 32, 24>;
+using P6144c = Plan<6144, 24, 16, 16>;  // half lines of the cluster-split row pass
 
 const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"),
                             RowOf<float, Rec<P12288>, 2, 512>::make("16.32.24r V2x512"),
@@ -15,7 +17,9 @@ const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"
                             RowOf<float, Rec<P12288>, 2, 768, 15>::make("16.32.24r V2x768 tma-in tma-out l2pf"),
                             RowOf<float, Rec<P12288>, 2, 768, 11>::make("16.32.24r V2x768 tma-in l2pf"),
                             RowOf<float, RecT<P12288>, 2, 768, 15>::make("16.32.24t V2x768 tma-in tma-out l2pf"),
-                            RowOf<float, RecT<P12288>, 2, 768, 14>::make("16.32.24t V2x768 tma-in tma-out")};
+                            RowOf<float, RecT<P12288>, 2, 768, 14>::make("16.32.24t V2x768 tma-in tma-out"),
+                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512>::make(
+                                "2x24.16.16t V2x256 cluster tma-in tma-out")};
 const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
                             ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),

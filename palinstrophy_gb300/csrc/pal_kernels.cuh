@@ -82,8 +82,6 @@ struct StepArgs {
   int dbg_wait0;
 };
 
-// Rows per TMA box of the row tiles: the largest power of two up to 256 that
-// divides the N/2 stored rows (box dimensions are at most 256).
 // Groups per TMA box of the planar column tile: the largest divisor of the
 // group count g that is at most 256 (a box dimension's limit).
 __host__ __device__ constexpr int col_box_groups(int g) {
@@ -92,6 +90,8 @@ __host__ __device__ constexpr int col_box_groups(int g) {
   return b;
 }
 
+// Rows per TMA box of the row tiles: the largest power of two up to 256 that
+// divides the N/2 stored rows (box dimensions are at most 256).
 __host__ __device__ constexpr int tma_box_rows(int nh) {
   int b = 256;
   while (b > 1 && nh % b != 0) b /= 2;
@@ -734,6 +734,44 @@ __device__ __forceinline__ void l2_prefetch_line(const void* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
+// The middle of the row pass: last inverse DIF pass -> products -> first
+// forward DIT pass, one smem round trip.  NEXTDT needs the CFL maximum; the
+// sum of u^2 + v^2 here only serves the finiteness check (a NaN drops out of a
+// max), so it is a plain sum in the working precision.  The diagnostic
+// mean(u^2 + v^2) is k_phys's compensated FP64 sum (pal_diagnostics).
+template <typename T, class PL, int V, int NT>
+__device__ __forceinline__ void row_products(cplx<T>* sm, int tid, bool stats, T& mx, T& acc) {
+  using C = cplx<T>;
+  constexpr int R = PL::RP;
+  constexpr int NB = V * (PL::M / R);
+  for (int w = tid; w < NB; w += NT) {
+    const int v = w % V;
+    const int b = w / V;
+    C* p = sm + b * (R + 1) * V + v;
+    C x[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) x[j] = p[j * V];
+    Dft<R, +1, C>::run(x);
+    if (stats) {
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const T u = x[j].x, q = x[j].y;
+        mx = fmax(mx, fabs(u) + fabs(q));
+        acc = fma(u, u, fma(q, q, acc));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const T u = x[j].x, q = x[j].y;
+      x[j] = C{u * u - q * q, u * q};
+    }
+    Dft<R, -1, C>::run(x);
+#pragma unroll
+    for (int j = 0; j < R; ++j) p[j * V] = x[j];
+  }
+  __syncthreads();
+}
+
 // k_row: U-state rows -> P-state rows (products), optional CFL statistics.
 // PF bit 0: the tile one wave ahead (blockIdx.x + a.ahead) is pulled into L2
 // first, so that the block that will run it finds its rows there.
@@ -781,44 +819,9 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
     row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
   }
   dif_range<T, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
-
-  // middle: last inverse DIF pass -> products -> first forward DIT pass
-  // NEXTDT needs the CFL maximum; the sum of u^2 + v^2 here only serves the
-  // finiteness check (a NaN drops out of a max), so it is a plain sum in the
-  // working precision.  The diagnostic mean(u^2 + v^2) is k_phys's compensated
-  // FP64 sum (pal_diagnostics).
   const bool stats = (a.flags & F_STATS) != 0;
   T mx = T(0), acc = T(0);
-  {
-    constexpr int R = PL::RP;
-    constexpr int NB = V * (M / R);
-    for (int w = tid; w < NB; w += NT) {
-      const int v = w % V;
-      const int b = w / V;
-      C* p = sm + b * (R + 1) * V + v;
-      C x[R];
-#pragma unroll
-      for (int j = 0; j < R; ++j) x[j] = p[j * V];
-      Dft<R, +1, C>::run(x);
-      if (stats) {
-#pragma unroll
-        for (int j = 0; j < R; ++j) {
-          const T u = x[j].x, q = x[j].y;
-          mx = fmax(mx, fabs(u) + fabs(q));
-          acc = fma(u, u, fma(q, q, acc));
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < R; ++j) {
-        const T u = x[j].x, q = x[j].y;
-        x[j] = C{u * u - q * q, u * q};
-      }
-      Dft<R, -1, C>::run(x);
-#pragma unroll
-      for (int j = 0; j < R; ++j) p[j * V] = x[j];
-    }
-    __syncthreads();
-  }
+  row_products<T, PL, V, NT>(sm, tid, stats, mx, acc);
   if constexpr (sizeof(C) == 8) {
     dit_range<T, PL, V, NT, -1, PL::NP - 2, 1>(sm, tw, tid);
     if constexpr ((PF & 4) != 0)

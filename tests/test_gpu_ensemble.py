@@ -258,3 +258,34 @@ def test_fused_passes_off_and_after_autotune(ts, monkeypatch):
     E = ts.Ensemble([256, 384], "fp32", 1e4, 0.5)
     assert not E.variant(384).startswith("fused")
     E.close()
+
+
+def test_cluster_split_rows_with_members(ts):
+    """Two N=8192 members run the autotuned cluster-split row pass (a tile per
+    2-CTA cluster, one grid row per member, TMA descriptors with a member
+    dimension) and step exactly like a single field on the same candidates."""
+    from palinstrophy_gb300 import _lib as L
+    if not L.supported(8192, "fp32"):
+        pytest.skip("fp32 is not compiled for N=8192")
+    Ns = [8192, 8192]
+    E = ts.Ensemble(Ns, "fp32", 1e5, 0.1)
+    assert "cluster" in E.variant(8192), E.variant(8192)
+    inits = [L.pao_generate(8192, 15.0, 1e5, sd, "KM3") for sd in (3, 4)]
+    for m, (om2, uc, st) in enumerate(inits):
+        E.set_member(m, om2, None, uc)
+        E.set_scalar(m, "visc", st["visc"])
+    E.init_dt()
+    E.step("LS_IMEX_RK3", 2, update=1, graph=True)
+    E.synchronize()
+    om2, uc, st = inits[1]
+    F = ts.Field(8192, "fp32", 1e5, 0.1)
+    F.set_state(om2, None, uc)
+    F.set_scalar("visc", st["visc"])
+    F.step2a()
+    F.set_scalar("dt", 0.1 / (F.compute_cflm() * math.pi))
+    F.step("LS_IMEX_RK3", 2, update=1)
+    assert F.variant()["desc"] == E.variant(8192)
+    assert np.array_equal(F.om2(), E.om2(1))
+    assert E.scalars(1)["dt"] == F.scalars()["dt"]
+    F.close()
+    E.close()

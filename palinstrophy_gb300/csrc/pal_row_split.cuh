@@ -101,6 +101,12 @@ __device__ __forceinline__ void static_for(F&& f, std::integer_sequence<int, J..
   (f(std::integral_constant<int, J>{}), ...);
 }
 
+// The same over J = B .. E-1.
+template <int B, class F, int... J>
+__device__ __forceinline__ void static_for_from(F&& f, std::integer_sequence<int, J...>) {
+  (f(std::integral_constant<int, B + J>{}), ...);
+}
+
 // Split twiddle e^{-2 pi i (i + jS) / M} of butterfly i, entry j: the loaded
 // e^{-2 pi i i / M} times the constant e^{-2 pi i j / (2R)} (S / M = 1 / (2R)).
 template <int R2, int J>
@@ -142,36 +148,74 @@ struct SplitGeom {
   static_assert(JP * PHASES == 2 * T3 && 2 * NBUF >= PHASES && NBUF < PHASES, "phases and buffers");
 };
 
+// Accumulates the rows of input phase P (j = P JP .. P JP + JP - 1) of work
+// item q into its butterflies' inputs x (butterfly q) and y (butterfly i2):
+// row k contributes Z[k] at position k and sg times its mirror
+// conj(u^[k]) + i conj(v^[k]) at position M/2 - k.  `ld(e)` reads element e of
+// the phase's [plane][row][v] staging buffer.
+template <class PL, int P, class LD>
+__device__ __forceinline__ void split_accumulate(float2 (&x)[SplitGeom<PL>::R], float2 (&y)[SplitGeom<PL>::R], LD&& ld,
+                                                 int q, int i2, int v, bool self, float sg) {
+  using C = float2;
+  using G = SplitGeom<PL>;
+  constexpr int R = G::R, S = G::S, ROWS = G::ROWS, JP = G::JP;
+  constexpr int V = 2;
+#pragma unroll
+  for (int jj = 0; jj < JP; ++jj) {
+    const int j = P * JP + jj;
+    {  // row q + jS: Z at position q + jS, the mirror at M/2 - q - jS
+      const int r = q + jj * S;
+      const C u = ld(r * V + v), w = ld((ROWS + r) * V + v);
+      const C d = (self && j == 0) ? C{u.x, w.x} : C{u.x - w.y, u.y + w.x};
+      const C m = C{sg * (u.x + w.y), sg * (w.x - u.y)};
+      x[j] = cadd(x[j], d);
+      if (self) {
+        if (j > 0) x[R - j] = cadd(x[R - j], m);
+      } else {
+        y[R - 1 - j] = cadd(y[R - 1 - j], m);
+      }
+    }
+    {  // row i2 + jS
+      const int r = i2 + jj * S;
+      const C u = ld(r * V + v), w = ld((ROWS + r) * V + v);
+      const C d = C{u.x - w.y, u.y + w.x};
+      const C m = C{sg * (u.x + w.y), sg * (w.x - u.y)};
+      y[j] = cadd(y[j], d);
+      if (self)
+        y[R - 1 - j] = cadd(y[R - 1 - j], m);
+      else
+        x[R - 1 - j] = cadd(x[R - 1 - j], m);
+    }
+  }
+}
+
+// Bounded wait for a phase's bulk copies; a wait that runs out is reported
+// (wait_timeout) and followed by a second bounded wait, so that the buffer is
+// not read or reused while copies may still land in it.
+__device__ __forceinline__ void split_wait(const StepArgs& a, unsigned long long* bar, unsigned parity, bool first,
+                                           int tid) {
+  if (!mbar_wait(bar, parity, (first && a.dbg_wait0) ? 0 : 1 << 22)) {
+    if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
+    mbar_wait(bar, parity, 1 << 22);
+  }
+}
+
 // First pass of the half-line inverse transform of CTA `rank` (see above).
-template <class PL, int V, int NT>
+// MC: input rows by multicast TMA loads (each CTA fetches one plane for both).
+// Without MC, CTA c TMA-loads only the rows c N/4 .. (c+1) N/4 - 1 of both
+// planes into its own shared memory and reads the other half of the rows from
+// its peer's through distributed shared memory.
+template <class PL, int V, int NT, bool MC>
 __device__ __forceinline__ void split_first_pass(const StepArgs& a, float2* sm, int z0, int tid, const TmaMaps& maps,
                                                  unsigned long long* bars, int member, unsigned rank,
                                                  const float2* __restrict__ sw) {
   using C = float2;
   using G = SplitGeom<PL>;
-  constexpr int R = G::R, S = G::S, ROWS = G::ROWS, JP = G::JP, BOX = G::BOX;
+  constexpr int R = G::R, S = G::S, ROWS = G::ROWS, BOX = G::BOX;
   constexpr int SP = PL::pstride(0);
-  static_assert(V * G::NQ == NT, "one work item per thread");
+  static_assert(V == 2 && V * G::NQ == NT, "two lines, one work item per thread");
   constexpr int NBUF = G::NBUF;
   static_assert(size_t(2) * NBUF * ROWS * V <= size_t(PL::PADM) * V, "the phase buffers fit in the tile");
-  // Phase p's rows of both planes land in buffer p % NBUF ([plane][row][v]) of
-  // both CTAs: CTA c fetches plane c's boxes and the TMA unit delivers each
-  // to the two CTAs, so every row is requested once per cluster.  Each CTA's
-  // mbarrier counts the bytes of both planes.  Phases NBUF.. refill the first
-  // buffers once both CTAs have consumed them: one cluster barrier.
-  auto issue = [&](int p) {
-    unsigned long long* bar = bars + (p % NBUF);
-    C* dst = sm + (size_t)(p % NBUF) * 2 * ROWS * V + (size_t)rank * ROWS * V;
-    const CUtensorMap* map = rank == 0 ? &maps.w0 : &maps.w1;
-    mbar_expect_tx(bar, 2u * ROWS * V * (unsigned)sizeof(C));
-#pragma unroll 1
-    for (int bx = 0; bx < ROWS / BOX; ++bx)
-      tma_load_3d_mc(map, dst + (size_t)bx * BOX * V, bar, 2 * z0, p * ROWS + bx * BOX, member, 0x3);
-  };
-  if (tid == 0) {
-#pragma unroll 1
-    for (int p = 0; p < NBUF; ++p) issue(p);
-  }
   const int v = tid % V;
   const int q = tid / V;
   const bool self = q == 0;
@@ -180,54 +224,84 @@ __device__ __forceinline__ void split_first_pass(const StepArgs& a, float2* sm, 
   C x[R], y[R];
 #pragma unroll
   for (int j = 0; j < R; ++j) x[j] = y[j] = C{0.0f, 0.0f};
-#pragma unroll
-  for (int p = 0; p < G::PHASES; ++p) {
-    unsigned long long* bar = bars + (p % NBUF);
-    const unsigned parity = (unsigned)(p / NBUF);
-    if (!mbar_wait(bar, parity, (p == 0 && a.dbg_wait0) ? 0 : 1 << 22)) {
-      // the copies did not complete in time: report it and wait (bounded) for
-      // them before the shared memory is read or reused
-      if (tid == 0) atomicExch(&a.sc->wait_timeout, 1);
-      mbar_wait(bar, parity, 1 << 22);
+  if constexpr (MC) {
+    // Phase p's rows of both planes land in buffer p % NBUF ([plane][row][v])
+    // of both CTAs: CTA c fetches plane c's boxes and the TMA unit delivers
+    // each to the two CTAs, so every row is requested once per cluster.  Each
+    // CTA's mbarrier counts the bytes of both planes.  Phases NBUF.. refill the
+    // first buffers once both CTAs have consumed them: one cluster barrier.
+    auto issue = [&](int p) {
+      unsigned long long* bar = bars + (p % NBUF);
+      C* dst = sm + (size_t)(p % NBUF) * 2 * ROWS * V + (size_t)rank * ROWS * V;
+      const CUtensorMap* map = rank == 0 ? &maps.w0 : &maps.w1;
+      mbar_expect_tx(bar, 2u * ROWS * V * (unsigned)sizeof(C));
+#pragma unroll 1
+      for (int bx = 0; bx < ROWS / BOX; ++bx)
+        tma_load_3d_mc(map, dst + (size_t)bx * BOX * V, bar, 2 * z0, p * ROWS + bx * BOX, member, 0x3);
+    };
+    if (tid == 0) {
+#pragma unroll 1
+      for (int p = 0; p < NBUF; ++p) issue(p);
     }
-    const C* stg = sm + (size_t)(p % NBUF) * 2 * ROWS * V;
-#pragma unroll
-    for (int jj = 0; jj < JP; ++jj) {
-      const int j = p * JP + jj;
-      {  // row q + jS: Z at position q + jS, the mirror at M/2 - q - jS
-        const int r = q + jj * S;
-        const C u = stg[(size_t)r * V + v], w = stg[(size_t)(ROWS + r) * V + v];
-        const C d = (self && j == 0) ? C{u.x, w.x} : C{u.x - w.y, u.y + w.x};
-        const C m = C{sg * (u.x + w.y), sg * (w.x - u.y)};
-        x[j] = cadd(x[j], d);
-        if (self) {
-          if (j > 0) x[R - j] = cadd(x[R - j], m);
-        } else {
-          y[R - 1 - j] = cadd(y[R - 1 - j], m);
+    static_for(
+        [&](auto pc) {
+          constexpr int p = decltype(pc)::value;
+          split_wait(a, bars + (p % NBUF), (unsigned)(p / NBUF), p == 0, tid);
+          const C* stg = sm + (size_t)(p % NBUF) * 2 * ROWS * V;
+          split_accumulate<PL, p>(x, y, [&](int e) { return stg[e]; }, q, i2, v, self, sg);
+          if (p == G::PHASES - NBUF - 1) {
+            // both CTAs are done with buffers 0 .. p before either refills them
+            __syncthreads();
+            cluster_arrive_relaxed();
+            cluster_wait();
+            if (tid == 0) {
+#pragma unroll 1
+              for (int pp = NBUF; pp < G::PHASES; ++pp) issue(pp);
+            }
+          }
+        },
+        std::make_integer_sequence<int, G::PHASES>{});
+  } else {
+    constexpr int HALF = G::PHASES / 2;  // phases per CTA: rows rank N/4 ..
+    static_assert(HALF <= NBUF, "a CTA's own phases fit in the buffers");
+    if (tid == 0) {
+#pragma unroll 1
+      for (int b = 0; b < HALF; ++b) {
+        const int p = (int)rank * HALF + b;
+        C* dst = sm + (size_t)b * 2 * ROWS * V;
+        mbar_expect_tx(bars + b, 2u * ROWS * V * (unsigned)sizeof(C));
+#pragma unroll 1
+        for (int bx = 0; bx < ROWS / BOX; ++bx) {
+          tma_load_3d(&maps.w0, dst + (size_t)bx * BOX * V, bars + b, 2 * z0, p * ROWS + bx * BOX, member);
+          tma_load_3d(&maps.w1, dst + (size_t)(ROWS + bx * BOX) * V, bars + b, 2 * z0, p * ROWS + bx * BOX, member);
         }
       }
-      {  // row i2 + jS
-        const int r = i2 + jj * S;
-        const C u = stg[(size_t)r * V + v], w = stg[(size_t)(ROWS + r) * V + v];
-        const C d = C{u.x - w.y, u.y + w.x};
-        const C m = C{sg * (u.x + w.y), sg * (w.x - u.y)};
-        y[j] = cadd(y[j], d);
-        if (self)
-          y[R - 1 - j] = cadd(y[R - 1 - j], m);
-        else
-          x[R - 1 - j] = cadd(x[R - 1 - j], m);
-      }
     }
-    if (p == G::PHASES - NBUF - 1) {
-      // both CTAs are done with buffers 0 .. p before either refills them
-      __syncthreads();
-      cluster_arrive_relaxed();
-      cluster_wait();
-      if (tid == 0) {
-#pragma unroll 1
-        for (int pp = NBUF; pp < G::PHASES; ++pp) issue(pp);
-      }
+    auto own = [&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      split_wait(a, bars + p % HALF, 0u, p % HALF == 0, tid);
+      const C* stg = sm + (size_t)(p % HALF) * 2 * ROWS * V;
+      split_accumulate<PL, p>(x, y, [&](int e) { return stg[e]; }, q, i2, v, self, sg);
+    };
+    auto peer = [&](auto pc) {
+      constexpr int p = decltype(pc)::value;
+      const unsigned base = peer_smem(sm + (size_t)(p % HALF) * 2 * ROWS * V, rank ^ 1u);
+      split_accumulate<PL, p>(x, y, [&](int e) { return ld_peer(base + (unsigned)e * 8u); }, q, i2, v, self, sg);
+    };
+    // own rows, then (once both CTAs' rows have landed and are published) the peer's
+    if (rank == 0) {
+      static_for(own, std::make_integer_sequence<int, HALF>{});
+      cluster_sync_publish(tid);
+      static_for_from<HALF>(peer, std::make_integer_sequence<int, HALF>{});
+    } else {
+      static_for_from<HALF>(own, std::make_integer_sequence<int, HALF>{});
+      cluster_sync_publish(tid);
+      static_for(peer, std::make_integer_sequence<int, HALF>{});
     }
+    // the peer has read this CTA's rows before the tile is overwritten
+    __syncthreads();
+    cluster_arrive_relaxed();
+    cluster_wait();
   }
   __syncthreads();  // the tile is free for the DFT outputs
   if (rank == 1) {  // the odd half: y_1[k] = (Z[k] - Z[k + M/2]) e^{+2 pi i k / M}
@@ -395,8 +469,9 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
 // k_row_split: the row pass of one tile (V lines of M = 2 PL::M points) by a
 // cluster of two CTAs.  Grid (2 M / V, members); blocks 2t and 2t + 1 are the
 // two halves of tile t.  The twiddle table holds the half-line plan's tables,
-// then the S split twiddles e^{-2 pi i p / M}, p < S.
-template <class PL, int V, int NT>
+// then the S split twiddles e^{-2 pi i p / M}, p < S.  MC: the input rows
+// arrive by multicast (split_first_pass).
+template <class PL, int V, int NT, bool MC>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
     k_row_split(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = float2;
@@ -414,10 +489,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
 #pragma unroll
     for (int b = 0; b < SplitGeom<PL>::NBUF; ++b) mbar_init(&bars[b], 1);
   }
-  // both CTAs' mbarriers are initialised before either multicasts into the other
-  cluster_arrive_relaxed();
-  cluster_wait();
-  split_first_pass<PL, V, NT>(a, sm, z0, tid, maps, bars, bk.y, rank, sw);
+  if constexpr (MC) {
+    // both CTAs' mbarriers are initialised before either multicasts into the other
+    cluster_arrive_relaxed();
+    cluster_wait();
+  } else {
+    __syncthreads();
+  }
+  split_first_pass<PL, V, NT, MC>(a, sm, z0, tid, maps, bars, bk.y, rank, sw);
   dif_range<float, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
   const bool stats = (a.flags & F_STATS) != 0;
   float mx = 0.0f, acc = 0.0f;
@@ -432,7 +511,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
 // Row candidate on the split kernel: PL is the half-line plan, PF the
 // full-line plan of k_phys (which needs physical rows in natural order).
 // Twiddle table: [PL tables | S split twiddles | PF tables].
-template <class PL, class PF, int V, int NT, int NTP>
+template <class PL, class PF, int V, int NT, int NTP, bool MC = true>
 struct RowSplitOf {
   static constexpr int M = 2 * PL::M;
   static_assert(PF::M == M, "the phys plan covers the whole line");
@@ -443,9 +522,9 @@ struct RowSplitOf {
   static constexpr int TW_ALL = TW_PHYS + PF::TW_TOTAL;
   static_assert(smem <= kSmemLimit && smem_phys <= kSmemLimit, "tiles fit in shared memory");
   static cudaError_t configure() {
-    cudaError_t e = cudaFuncSetAttribute(k_row_split<PL, V, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_row_split<PL, V, NT, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_row_split<PL, V, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(k_row_split<PL, V, NT, MC>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_phys<float, PF, V, NTP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -453,7 +532,7 @@ struct RowSplitOf {
   }
   static void row(const StepArgs& a, cudaStream_t s) {
     static const TmaMaps none{};
-    k_row_split<PL, V, NT><<<dim3(2 * M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
+    k_row_split<PL, V, NT, MC><<<dim3(2 * M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
         a, a.tmaps ? *a.tmaps : none);
   }
   static void phys(const StepArgs& a, cudaStream_t s) {
@@ -469,7 +548,7 @@ struct RowSplitOf {
   }
   static int blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_row_split<PL, V, NT>, NT, smem) == cudaSuccess) return n;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_row_split<PL, V, NT, MC>, NT, smem) == cudaSuccess) return n;
     (void)cudaGetLastError();  // a refused query must not read as a failed launch later
     return -1;
   }

@@ -470,8 +470,10 @@ def _precision_form(steps=2000, update=100):
 
 def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100):
     """N=8192 FP32 (KM3 K0=15 seed 4895, Re=1e5, LS-IMEX-RK3, CFL 0.1): steps/s and
-    per-kernel rates; and the energy / enstrophy history of the N=4096 FP32 form
-    against the FP64 plain run over 500 steps from the identical start."""
+    per-kernel rates; the energy / enstrophy history of the N=4096 FP32 form
+    against the FP64 plain run over 500 steps from the identical start; and
+    500 N=8192 FP32 steps of the same flow against that FP64 run."""
+    import numpy as np
     import torch
     from palinstrophy_gb300 import _lib as L
     from palinstrophy_gb300.turbo_simulator import Field
@@ -499,22 +501,65 @@ def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100
            "kernels": variant,
            "k_row": {"ms": ms_row, "algorithmic_GBps": 6.0 * n2 * s_bytes / (ms_row / 1000.0) / 1e9},
            "k_col": {"ms": ms_col, "algorithmic_GBps": (25.0 / 3.0) * n2 * s_bytes / (ms_col / 1000.0) / 1e9}}
+    # N=4096 histories, sampled every `fine` steps (NEXTDT follows the global
+    # iteration count, so the sampling does not change the trajectory)
+    fine = 10
     hist = {}
     for prec in ("fp32", "fp64"):
         G = _field(prec, om2, uc, visc)
         h = []
-        for _ in range(drift_steps // every):
-            G.step(METHOD, every, update=UPDATE, final_update=True)
+        for _ in range(drift_steps // fine):
+            G.step(METHOD, fine, update=UPDATE, final_update=False)
             d = G.diagnostics()
-            h.append((d["E"], d["Z"]))
+            h.append((G.scalars()["t"], d["E"], d["Z"]))
         hist[prec] = h
         G.close()
-    dE = max(abs(a[0] / b[0] - 1.0) for a, b in zip(hist["fp32"], hist["fp64"]))
-    dZ = max(abs(a[1] / b[1] - 1.0) for a, b in zip(hist["fp32"], hist["fp64"]))
+    coarse = {p: hist[p][every // fine - 1::every // fine] for p in hist}
+    dE = max(abs(a[1] / b[1] - 1.0) for a, b in zip(coarse["fp32"], coarse["fp64"]))
+    dZ = max(abs(a[2] / b[2] - 1.0) for a, b in zip(coarse["fp32"], coarse["fp64"]))
     drift = {"N": N_GRID, "steps": drift_steps, "every": every,
-             "E_fp64": [h[0] for h in hist["fp64"]], "Z_fp64": [h[1] for h in hist["fp64"]],
+             "E_fp64": [h[1] for h in coarse["fp64"]], "Z_fp64": [h[2] for h in coarse["fp64"]],
              "max_rel_dE_fp32_vs_fp64": dE, "max_rel_dZ_fp32_vs_fp64": dZ}
-    return {"N8192_fp32": big, "N4096_fp32_vs_fp64_history": drift}
+    # N=8192 FP32 from the same flow: the N=4096 start embedded in the larger
+    # spectral grid (coefficients are grid-independent: irfft2 norm="forward";
+    # the kz = -N/2 row, which the N=4096 step keeps at zero, stays zero), 500
+    # steps; E and Z against the N=4096 FP64 run at the same physical times
+    # (linear interpolation between its samples, dt being half as large here)
+    h4 = N_GRID // 2
+    big_om2 = np.zeros((N, N // 2), dtype=np.complex64)
+    big_om2[:h4, :h4] = om2[:h4, :]
+    big_om2[N - h4 + 1:, :h4] = om2[h4 + 1:, :]
+    H = Field(N, "fp32", RE, CFL)
+    H.set_state(big_om2, None, None)
+    H.set_scalar("visc", visc)
+    H.step2a()
+    H.set_scalar("dt", CFL / (H.compute_cflm() * math.pi))
+    H.set_scalar("cn", 1.0)
+    H.set_scalar("cnm1", 0.0)
+    d0 = H.diagnostics()
+    h8 = []
+    for _ in range(drift_steps // every):
+        H.step(METHOD, every, update=UPDATE, final_update=True)
+        d = H.diagnostics()
+        h8.append((H.scalars()["t"], d["E"], d["Z"]))
+    H.close()
+    t64 = np.array([0.0] + [h[0] for h in hist["fp64"]])
+    E64 = np.array([np.nan] + [h[1] for h in hist["fp64"]])
+    Z64 = np.array([np.nan] + [h[2] for h in hist["fp64"]])
+    G = _field("fp64", om2, uc, visc)
+    d64 = G.diagnostics()
+    G.close()
+    E64[0], Z64[0] = d64["E"], d64["Z"]
+    cross = {"N": N, "dtype": "f32", "steps": drift_steps, "every": every,
+             "start": "the N=4096 KM3 start (K0=15, seed 4895) embedded in the N=8192 spectral grid",
+             "t": [h[0] for h in h8], "E": [h[1] for h in h8], "Z": [h[2] for h in h8],
+             "drift_E": h8[-1][1] / d0["E"] - 1.0, "drift_Z": h8[-1][2] / d0["Z"] - 1.0,
+             "fp64_N4096_drift_E_same_t": float(np.interp(h8[-1][0], t64, E64)) / d64["E"] - 1.0,
+             "fp64_N4096_drift_Z_same_t": float(np.interp(h8[-1][0], t64, Z64)) / d64["Z"] - 1.0,
+             "max_rel_dE_vs_fp64_N4096": max(abs(h[1] / float(np.interp(h[0], t64, E64)) - 1.0) for h in h8),
+             "max_rel_dZ_vs_fp64_N4096": max(abs(h[2] / float(np.interp(h[0], t64, Z64)) - 1.0) for h in h8),
+             "rel_E0_vs_N4096": d0["E"] / d64["E"] - 1.0, "rel_Z0_vs_N4096": d0["Z"] / d64["Z"] - 1.0}
+    return {"N8192_fp32": big, "N4096_fp32_vs_fp64_history": drift, "N8192_fp32_vs_N4096_fp64_history": cross}
 
 
 def _generator_times(N=N_GRID):

@@ -380,8 +380,11 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
   }
   __syncthreads();  // every read of the tile is done
   C* stg = sm;      // output staging [plane][row - rank N/4][v]
-  // send slots [slot][tid]: CTA 0's beside its staging, CTA 1's over it
-  C* snd = rank == 0 ? sm + (size_t)2 * OUT * V : sm;
+  // send slots [slot][tid]: CTA 0's beside its staging; CTA 1's at the top of
+  // the tile, above its A-plane staging but over part of its B-plane staging
+  constexpr size_t SND1 = size_t(PL::PADM) * V - size_t(G::SEND1) * NT;
+  static_assert(SND1 >= size_t(OUT) * V, "CTA 1's send slots lie above its A-plane staging");
+  C* snd = rank == 0 ? sm + (size_t)2 * OUT * V : sm + SND1;
   if (rank == 0) {  // what CTA 1 reads: y1[T3 .. 2T3], y2[T3 .. 2T3)
 #pragma unroll
     for (int s = 0; s < T3; ++s) {
@@ -399,7 +402,14 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
     }
   }
   cluster_sync_publish(tid);  // (1) the send slots are written
-  const unsigned peer = peer_smem(rank == 0 ? sm : sm + (size_t)2 * OUT * V, rank ^ 1u) + (unsigned)tid * 8u;
+  const unsigned peer = peer_smem(rank == 0 ? sm + SND1 : sm + (size_t)2 * OUT * V, rank ^ 1u) + (unsigned)tid * 8u;
+  // bulk tensor stores of one plane of this CTA's output rows
+  auto store_plane = [&](int plane) {
+#pragma unroll 1
+    for (int bx = 0; bx < OUT / BOX; ++bx)
+      tma_store_3d(plane == 0 ? &maps.w0 : &maps.w1, stg + (size_t)(plane * OUT + bx * BOX) * V, 2 * z0,
+                   (int)rank * OUT + bx * BOX, member);
+  };
   auto slot = [&](int s) { return ld_peer(peer + (unsigned)s * NT * 8u); };
   const C aq = __ldg(sw + q), ai = __ldg(sw + i2);
   if (rank == 0) {
@@ -424,6 +434,15 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
     }, std::make_integer_sequence<int, T3>{});
     __syncthreads();           // every read of the peer's slots has returned
     cluster_arrive_relaxed();  // (2) done with the peer's slots
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      store_plane(0);
+      store_plane(1);
+      tma_commit();
+      tma_wait_read();
+    }
+    cluster_wait();  // keep the send slots until CTA 1 has read them
   } else {
     // rows q + jS and i2 + jS, T3 <= j < 2T3: peer G_0, own G_1
     C A1[T3], B1[T3], A2[T3], B2[T3];
@@ -439,31 +458,33 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
       split_combine(g0, y1[j], h0, self ? y1[e] : y2[R - 1 - j], split_tw<2 * R, j>(aq), A1[t], B1[t]);
       split_combine(g0b, y2[j], h0b, self ? y2[R - 1 - j] : y1[R - 1 - j], split_tw<2 * R, j>(ai), A2[t], B2[t]);
     }, std::make_integer_sequence<int, T3>{});
-    __syncthreads();           // every read of the peer's slots has returned
-    cluster_arrive_relaxed();  // (2) done with the peer's slots
-    cluster_wait();            // ... and the peer with ours: the tile is free for staging
+    // the A plane's staging lies below the send slots: write and store it now
 #pragma unroll
     for (int t = 0; t < T3; ++t) {
-      const int r1 = q + t * S, r2 = i2 + t * S;  // rows k - N/4
-      stg[(size_t)r1 * V + v] = A1[t];
-      stg[(size_t)(OUT + r1) * V + v] = B1[t];
-      stg[(size_t)r2 * V + v] = A2[t];
-      stg[(size_t)(OUT + r2) * V + v] = B2[t];
+      stg[(size_t)(q + t * S) * V + v] = A1[t];  // rows k - N/4
+      stg[(size_t)(i2 + t * S) * V + v] = A2[t];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();  // ... and every read of the peer's slots has returned
+    if (tid == 0) {
+      store_plane(0);
+      tma_commit();
+    }
+    cluster_arrive_relaxed();  // (2) done with the peer's slots
+    cluster_wait();            // ... and the peer with ours: the B-plane staging is free
+#pragma unroll
+    for (int t = 0; t < T3; ++t) {
+      stg[(size_t)(OUT + q + t * S) * V + v] = B1[t];
+      stg[(size_t)(OUT + i2 + t * S) * V + v] = B2[t];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      store_plane(1);
+      tma_commit();
+      tma_wait_read();  // both planes' stores have read the tile
     }
   }
-  fence_proxy_async_smem();
-  __syncthreads();
-  if (tid == 0) {
-#pragma unroll 1
-    for (int bx = 0; bx < OUT / BOX; ++bx) {
-      tma_store_3d(&maps.w0, stg + (size_t)bx * BOX * V, 2 * z0, (int)rank * OUT + bx * BOX, member);
-      tma_store_3d(&maps.w1, stg + (size_t)(OUT + bx * BOX) * V, 2 * z0, (int)rank * OUT + bx * BOX, member);
-    }
-    tma_commit();
-    tma_wait_read();
-  }
-  // CTA 0 keeps its shared memory until CTA 1 has read its send slots
-  if (rank == 0) cluster_wait();
 }
 
 // k_row_split: the row pass of one tile (V lines of M = 2 PL::M points) by a

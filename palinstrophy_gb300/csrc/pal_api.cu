@@ -339,7 +339,9 @@ int autotune(pal_handle* h) {
       return PAL_OK;
     };
     float best = 1e30f;
+    const bool mc_ok = pal::tma_multicast_allowed();
     for (int r = 0; r < h->ks->n_rows; ++r) {
+      if (h->ks->rows[r].multicast && !mc_ok) continue;
       if (int rc = select_variant(h, r, 0)) return rc;
       const StepArgs a = base_args(h);
       float ms = 0.f;

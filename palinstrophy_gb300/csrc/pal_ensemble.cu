@@ -428,6 +428,7 @@ int pal_ensemble_autotune(pal_ensemble* e) {
     const pal::RowKernels* best_r = g.rk;
     for (int q = 0; q < g.ks->n_rows && rc == PAL_OK; ++q) {
       const pal::RowKernels* rk = &g.ks->rows[q];
+      if (rk->multicast && !pal::tma_multicast_allowed()) continue;
       if (rk->configure() != cudaSuccess) continue;
       if (rk->tma && !pal::encode_row_maps(&g.tmaps, g.w0, g.w1, g.N, rk->V, nm)) continue;
       rk->twiddles(g.tw_row, e->stream);

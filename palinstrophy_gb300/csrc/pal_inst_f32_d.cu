@@ -18,10 +18,12 @@ const RowKernels r8192[] = {RowOf<float, P12288, 2, 256>::make("16.32.24 V2x256"
                             RowOf<float, Rec<P12288>, 2, 768, 11>::make("16.32.24r V2x768 tma-in l2pf"),
                             RowOf<float, RecT<P12288>, 2, 768, 15>::make("16.32.24t V2x768 tma-in tma-out l2pf"),
                             RowOf<float, RecT<P12288>, 2, 768, 14>::make("16.32.24t V2x768 tma-in tma-out"),
-                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512>::make(
-                                "2x24.16.16t V2x256 cluster tma-in tma-out"),
-                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512, false>::make(
-                                "2x24.16.16t V2x256 cluster tma-in dsmem tma-out")};
+                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512, SPLIT_MULTICAST>::make(
+                                "2x24.16.16t V2x256 cluster tma-in mc tma-out"),
+                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512, SPLIT_HALVES>::make(
+                                "2x24.16.16t V2x256 cluster tma-in dsmem tma-out"),
+                            RowSplitOf<RecT<P6144c>, Rec<P12288>, 2, 256, 512, SPLIT_LOAD_ALL>::make(
+                                "2x24.16.16t V2x256 cluster tma-in tma-out")};
 const ColKernels c8192[] = {ColOf<float, P12288, 512>::make("16.32.24 x512"),
                             ColOf<float, Rec<P12288>, 512>::make("16.32.24r x512"),
                             ColOf<float, Rec<P12288>, 512, 2>::make("16.32.24r x512 hoist"),

@@ -7,6 +7,8 @@
 // twiddle tables.  pal_create times every candidate on the handle's own state
 // and keeps the fastest (pal_autotune in pal_api.cu).
 #pragma once
+#include <cstdlib>
+
 #include "pal_adjoint.cuh"
 #include "pal_kernels.cuh"
 
@@ -23,6 +25,7 @@ struct RowKernels {
   void (*phys)(const StepArgs&, cudaStream_t);
   void (*twiddles)(void* tw, cudaStream_t);
   int (*blocks_per_sm)();  // resident k_row blocks per SM (occupancy calculator)
+  bool multicast = false;  // loads by TMA cluster multicast (left out of tuning by PAL_TMA_MULTICAST=0)
 };
 
 struct ColKernels {
@@ -73,6 +76,13 @@ struct KernelSet {
                  cudaStream_t);
   const AdjKernels* adj;  // nullptr where no adjoint is compiled
 };
+
+// Whether the autotuners may pick row candidates that load by TMA cluster
+// multicast: yes unless PAL_TMA_MULTICAST=0.
+inline bool tma_multicast_allowed() {
+  const char* e = std::getenv("PAL_TMA_MULTICAST");
+  return !(e && e[0] == '0');
+}
 
 constexpr int kSpectralThreads = 256;
 constexpr size_t kSmemLimit = 227 * 1024;

@@ -200,12 +200,17 @@ __device__ __forceinline__ void split_wait(const StepArgs& a, unsigned long long
   }
 }
 
-// First pass of the half-line inverse transform of CTA `rank` (see above).
-// MC: input rows by multicast TMA loads (each CTA fetches one plane for both).
-// Without MC, CTA c TMA-loads only the rows c N/4 .. (c+1) N/4 - 1 of both
-// planes into its own shared memory and reads the other half of the rows from
-// its peer's through distributed shared memory.
-template <class PL, int V, int NT, bool MC>
+// How the input rows reach the two CTAs of a split row tile.
+enum SplitLoad {
+  SPLIT_LOAD_ALL = 0,   // each CTA TMA-loads every row into its own shared memory
+  SPLIT_MULTICAST = 1,  // each CTA fetches one plane by multicast TMA, delivered to both
+  SPLIT_HALVES = 2,     // CTA c TMA-loads rows c N/4 .. (c+1) N/4 - 1 and reads the
+                        // other half from its peer through distributed shared memory
+};
+
+// First pass of the half-line inverse transform of CTA `rank` (see above),
+// input rows as LOAD says.
+template <class PL, int V, int NT, int LOAD>
 __device__ __forceinline__ void split_first_pass(const StepArgs& a, float2* sm, int z0, int tid, const TmaMaps& maps,
                                                  unsigned long long* bars, int member, unsigned rank,
                                                  const float2* __restrict__ sw) {
@@ -224,20 +229,31 @@ __device__ __forceinline__ void split_first_pass(const StepArgs& a, float2* sm, 
   C x[R], y[R];
 #pragma unroll
   for (int j = 0; j < R; ++j) x[j] = y[j] = C{0.0f, 0.0f};
-  if constexpr (MC) {
-    // Phase p's rows of both planes land in buffer p % NBUF ([plane][row][v])
-    // of both CTAs: CTA c fetches plane c's boxes and the TMA unit delivers
-    // each to the two CTAs, so every row is requested once per cluster.  Each
-    // CTA's mbarrier counts the bytes of both planes.  Phases NBUF.. refill the
-    // first buffers once both CTAs have consumed them: one cluster barrier.
+  if constexpr (LOAD != SPLIT_HALVES) {
+    // Phase p's rows of both planes land in buffer p % NBUF ([plane][row][v]).
+    // SPLIT_MULTICAST: CTA c fetches plane c's boxes and the TMA unit delivers
+    // each to the two CTAs, so every row is requested once per cluster; each
+    // CTA's mbarrier counts the bytes of both planes.  SPLIT_LOAD_ALL: each
+    // CTA fetches both planes itself.  Phases NBUF.. refill the first buffers
+    // once they are consumed: by both CTAs (a cluster barrier) when the peer
+    // writes into them too, else by this CTA's threads.
     auto issue = [&](int p) {
       unsigned long long* bar = bars + (p % NBUF);
-      C* dst = sm + (size_t)(p % NBUF) * 2 * ROWS * V + (size_t)rank * ROWS * V;
-      const CUtensorMap* map = rank == 0 ? &maps.w0 : &maps.w1;
+      C* buf = sm + (size_t)(p % NBUF) * 2 * ROWS * V;
       mbar_expect_tx(bar, 2u * ROWS * V * (unsigned)sizeof(C));
+      if constexpr (LOAD == SPLIT_MULTICAST) {
+        const CUtensorMap* map = rank == 0 ? &maps.w0 : &maps.w1;
 #pragma unroll 1
-      for (int bx = 0; bx < ROWS / BOX; ++bx)
-        tma_load_3d_mc(map, dst + (size_t)bx * BOX * V, bar, 2 * z0, p * ROWS + bx * BOX, member, 0x3);
+        for (int bx = 0; bx < ROWS / BOX; ++bx)
+          tma_load_3d_mc(map, buf + (size_t)(rank * ROWS + bx * BOX) * V, bar, 2 * z0, p * ROWS + bx * BOX, member,
+                         0x3);
+      } else {
+#pragma unroll 1
+        for (int bx = 0; bx < ROWS / BOX; ++bx) {
+          tma_load_3d(&maps.w0, buf + (size_t)bx * BOX * V, bar, 2 * z0, p * ROWS + bx * BOX, member);
+          tma_load_3d(&maps.w1, buf + (size_t)(ROWS + bx * BOX) * V, bar, 2 * z0, p * ROWS + bx * BOX, member);
+        }
+      }
     };
     if (tid == 0) {
 #pragma unroll 1
@@ -250,10 +266,12 @@ __device__ __forceinline__ void split_first_pass(const StepArgs& a, float2* sm, 
           const C* stg = sm + (size_t)(p % NBUF) * 2 * ROWS * V;
           split_accumulate<PL, p>(x, y, [&](int e) { return stg[e]; }, q, i2, v, self, sg);
           if (p == G::PHASES - NBUF - 1) {
-            // both CTAs are done with buffers 0 .. p before either refills them
+            // buffers 0 .. p are consumed (by both CTAs, if the peer refills them too)
             __syncthreads();
-            cluster_arrive_relaxed();
-            cluster_wait();
+            if constexpr (LOAD == SPLIT_MULTICAST) {
+              cluster_arrive_relaxed();
+              cluster_wait();
+            }
             if (tid == 0) {
 #pragma unroll 1
               for (int pp = NBUF; pp < G::PHASES; ++pp) issue(pp);
@@ -490,9 +508,9 @@ __device__ __forceinline__ void split_last_pass(const StepArgs& a, float2* sm, i
 // k_row_split: the row pass of one tile (V lines of M = 2 PL::M points) by a
 // cluster of two CTAs.  Grid (2 M / V, members); blocks 2t and 2t + 1 are the
 // two halves of tile t.  The twiddle table holds the half-line plan's tables,
-// then the S split twiddles e^{-2 pi i p / M}, p < S.  MC: the input rows
-// arrive by multicast (split_first_pass).
-template <class PL, int V, int NT, bool MC>
+// then the S split twiddles e^{-2 pi i p / M}, p < S.  LOAD: how the input
+// rows arrive (SplitLoad).
+template <class PL, int V, int NT, int LOAD>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
     k_row_split(StepArgs a0, const __grid_constant__ TmaMaps maps) {
   using C = float2;
@@ -510,14 +528,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
 #pragma unroll
     for (int b = 0; b < SplitGeom<PL>::NBUF; ++b) mbar_init(&bars[b], 1);
   }
-  if constexpr (MC) {
+  if constexpr (LOAD == SPLIT_MULTICAST) {
     // both CTAs' mbarriers are initialised before either multicasts into the other
     cluster_arrive_relaxed();
     cluster_wait();
   } else {
     __syncthreads();
   }
-  split_first_pass<PL, V, NT, MC>(a, sm, z0, tid, maps, bars, bk.y, rank, sw);
+  split_first_pass<PL, V, NT, LOAD>(a, sm, z0, tid, maps, bars, bk.y, rank, sw);
   dif_range<float, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
   const bool stats = (a.flags & F_STATS) != 0;
   float mx = 0.0f, acc = 0.0f;
@@ -532,7 +550,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2)
 // Row candidate on the split kernel: PL is the half-line plan, PF the
 // full-line plan of k_phys (which needs physical rows in natural order).
 // Twiddle table: [PL tables | S split twiddles | PF tables].
-template <class PL, class PF, int V, int NT, int NTP, bool MC = true>
+template <class PL, class PF, int V, int NT, int NTP, int LOAD>
 struct RowSplitOf {
   static constexpr int M = 2 * PL::M;
   static_assert(PF::M == M, "the phys plan covers the whole line");
@@ -543,9 +561,9 @@ struct RowSplitOf {
   static constexpr int TW_ALL = TW_PHYS + PF::TW_TOTAL;
   static_assert(smem <= kSmemLimit && smem_phys <= kSmemLimit, "tiles fit in shared memory");
   static cudaError_t configure() {
-    cudaError_t e = cudaFuncSetAttribute(k_row_split<PL, V, NT, MC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_row_split<PL, V, NT, LOAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_row_split<PL, V, NT, MC>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(k_row_split<PL, V, NT, LOAD>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(k_phys<float, PF, V, NTP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -553,7 +571,7 @@ struct RowSplitOf {
   }
   static void row(const StepArgs& a, cudaStream_t s) {
     static const TmaMaps none{};
-    k_row_split<PL, V, NT, MC><<<dim3(2 * M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
+    k_row_split<PL, V, NT, LOAD><<<dim3(2 * M / V, a.members > 1 ? a.members : 1), NT, smem, s>>>(
         a, a.tmaps ? *a.tmaps : none);
   }
   static void phys(const StepArgs& a, cudaStream_t s) {
@@ -569,12 +587,13 @@ struct RowSplitOf {
   }
   static int blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_row_split<PL, V, NT, MC>, NT, smem) == cudaSuccess) return n;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_row_split<PL, V, NT, LOAD>, NT, smem) == cudaSuccess) return n;
     (void)cudaGetLastError();  // a refused query must not read as a failed launch later
     return -1;
   }
   static constexpr RowKernels make(const char* name) {
-    return RowKernels{name, V, NT, true, smem, TW_ALL, configure, row, phys, twiddles, blocks_per_sm};
+    return RowKernels{name, V, NT, true, smem, TW_ALL, configure, row, phys, twiddles, blocks_per_sm,
+                      LOAD == SPLIT_MULTICAST};
   }
 };
 

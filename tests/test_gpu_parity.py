@@ -568,3 +568,24 @@ def test_diagnostic_sums_are_compensated_fp64(ts, prec):
     for k in ("E", "Z", "P"):
         assert abs(d[k] / sp[k] - 1.0) <= 1e-10, (k, d[k], sp[k])
     F.close()
+
+
+def test_multicast_candidates_can_be_left_out(ts):
+    """PAL_TMA_MULTICAST=0 keeps the autotuner off the row candidates that load
+    by TMA cluster multicast (read when a size is first tuned in a process,
+    hence a fresh interpreter)."""
+    import os
+    import subprocess
+    import sys
+    from palinstrophy_gb300 import _lib as L
+    if not L.supported(8192, "fp32"):
+        pytest.skip("fp32 is not compiled for N=8192")
+    code = ("from palinstrophy_gb300.turbo_simulator import Field\n"
+            "F = Field(8192, 'fp32', 1e5, 0.1)\n"
+            "print(F.variant()['desc'])\n"
+            "F.close()\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, check=True,
+                         env={**os.environ, "PAL_TMA_MULTICAST": "0"}, timeout=600)
+    desc = out.stdout.strip().splitlines()[-1]
+    assert desc.startswith("row[") and " mc " not in desc, desc

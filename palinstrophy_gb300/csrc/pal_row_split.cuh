@@ -23,9 +23,11 @@
 // lacks from its peer's shared memory (distributed shared memory), so no
 // intermediate line ever goes back to global memory.
 //
-// Input rows reach both CTAs by multicast TMA bulk tensor loads (each row
-// requested once per cluster) in eight phases of N/16 rows over six buffers,
-// and the first DIF pass (radix R = PL::R[0], stride
+// Input rows reach the CTAs by TMA bulk tensor loads in eight phases of N/16
+// rows over six buffers, in one of three forms (SplitLoad): multicast (each
+// row requested once per cluster and delivered to both CTAs), each CTA
+// loading every row, or each CTA loading a quarter of the rows and reading the
+// other quarter from its peer.  The first DIF pass (radix R = PL::R[0], stride
 // S = M / (2R)) accumulates every row's two contributions (Z[k] at position k
 // and the mirrored entry conj(u^[k]) + i conj(v^[k]) at position M/2 - k) in
 // registers, item by item as in row_first_pass_tma: work item q < S/2 owns
@@ -50,7 +52,6 @@ __device__ __forceinline__ unsigned cluster_rank() {
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
   return r;
 }
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 // Arrive without release semantics: for the points where the accesses to be
 // ordered are this CTA's own shared-memory reads, which the CTA barrier just

@@ -468,6 +468,20 @@ def _precision_form(steps=2000, update=100):
     return out
 
 
+def _embed_spectrum(om2, N):
+    """A compact (n, n/2) rfft2 band (kz in fftfreq order, kx < n/2, amplitudes
+    as irfft2(norm="forward") reads them) placed in the (N, N/2) band of a
+    larger grid: the same field.  The kz = -n/2 row, which the n-grid step
+    keeps at zero, is left at zero."""
+    import numpy as np
+    n = om2.shape[0]
+    h = n // 2
+    out = np.zeros((N, N // 2), dtype=om2.dtype)
+    out[:h, :h] = om2[:h, :]
+    out[N - h + 1:, :h] = om2[h + 1:, :]
+    return out
+
+
 def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100):
     """N=8192 FP32 (KM3 K0=15 seed 4895, Re=1e5, LS-IMEX-RK3, CFL 0.1): steps/s and
     per-kernel rates; the energy / enstrophy history of the N=4096 FP32 form
@@ -525,10 +539,7 @@ def _large_single_field(om2, uc, visc, steps_8192=30, drift_steps=500, every=100
     # the kz = -N/2 row, which the N=4096 step keeps at zero, stays zero), 500
     # steps; E and Z against the N=4096 FP64 run at the same physical times
     # (linear interpolation between its samples, dt being half as large here)
-    h4 = N_GRID // 2
-    big_om2 = np.zeros((N, N // 2), dtype=np.complex64)
-    big_om2[:h4, :h4] = om2[:h4, :]
-    big_om2[N - h4 + 1:, :h4] = om2[h4 + 1:, :]
+    big_om2 = _embed_spectrum(om2, N)
     H = Field(N, "fp32", RE, CFL)
     H.set_state(big_om2, None, None)
     H.set_scalar("visc", visc)

@@ -91,3 +91,26 @@ def test_oracle_process_round_trip():
     assert log[0, 0] == dt0 and len(log) == 1 + len(ref_log)
     assert [int(r[0]) for r in log[1:]] == [1, 5]
     assert secs > 0 and threads >= 1
+
+
+def test_spectral_embedding_keeps_the_field():
+    """The N=8192 comparison run starts from the N=4096 field embedded in the
+    larger spectral grid: sampled on the coarse grid it is the same field."""
+    import numpy as np
+    import bench
+    rng = np.random.default_rng(3)
+    n, N = 32, 64
+    om2 = (rng.standard_normal((n, n // 2)) + 1j * rng.standard_normal((n, n // 2))).astype(np.complex128)
+    om2[n // 2, :] = 0.0                         # the kz = -n/2 row the n-grid step keeps at zero
+    om2[0, 0] = om2[0, 0].real                   # Hermitian on the kx = 0 column
+    om2[n - np.arange(1, n // 2), 0] = np.conj(om2[np.arange(1, n // 2), 0])
+    big = bench._embed_spectrum(om2, N)
+    assert big.shape == (N, N // 2)
+
+    def field(c, m):
+        full = np.zeros((m, m // 2 + 1), dtype=np.complex128)
+        full[:, : c.shape[1]] = c
+        return np.fft.irfft2(full, s=(m, m), norm="forward")
+
+    small, large = field(om2, n), field(big, N)
+    assert np.allclose(large[::2, ::2], small, atol=1e-12)

@@ -69,3 +69,45 @@ def test_timed_out_wait_is_reported_and_cleared(ts, N):
         B.set_debug(7, 1)
     A.close()
     B.close()
+
+
+@pytest.mark.parametrize("form", ["cluster tma-in mc tma-out", "cluster tma-in dsmem tma-out", "cluster tma-in tma-out"])
+def test_cluster_split_timed_out_wait(ts, form):
+    """The cluster-split N=8192 row pass in each of its input forms: a first
+    phase wait given no polls is reported once as PAL_ERR_TIMEOUT, both CTAs
+    still wait for their copies and meet at every cluster barrier, and the
+    field equals an undisturbed run."""
+    from palinstrophy_gb300 import _lib as L
+    N = 8192
+    if not L.supported(N, "fp32"):
+        pytest.skip("fp32 is not compiled for N=8192")
+    om2, uc, st = L.pao_generate(N, 15.0, 1e5, 4895, "KM3")
+    fields = []
+    for _ in range(2):
+        F = ts.Field(N, "fp32", 1e5, 0.1)
+        v = F.variant()
+        idx = None
+        for r in range(v["n_rows"]):
+            F.set_variant(r, 0)
+            if F.variant()["desc"].split(" col[")[0].endswith(form + "]"):
+                idx = r
+        assert idx is not None, form
+        F.set_variant(idx, 0)
+        F.set_state(om2, None, uc)
+        F.set_scalar("visc", st["visc"])
+        F.step2a()
+        F.set_scalar("dt", 0.1 / (F.compute_cflm() * math.pi))
+        F.set_scalar("cn", 1.0)
+        F.set_scalar("cnm1", 0.0)
+        fields.append(F)
+    A, B = fields
+    A.step("LS_IMEX_RK3", 1, update=0)
+    B.set_debug(L.PAL_DBG_SKIP_FIRST_WAIT, 1)
+    B.step("LS_IMEX_RK3", 1, update=0)
+    with pytest.raises(L.PalError) as err:
+        B.scalars()
+    assert err.value.code == L.PAL_ERR_TIMEOUT
+    B.scalars()
+    assert np.array_equal(A.om2(), B.om2())
+    A.close()
+    B.close()

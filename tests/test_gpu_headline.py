@@ -12,7 +12,9 @@ comparison measures the step's arithmetic alone:
   the GPU's own NEXTDT after step 1 (CFLM, dt, cn) vs the oracle's: 1e-12 FP64
 
 N=2048 (the TMA column and row candidates at a second size), 10 steps, the
-same checks.  The oracle costs a few seconds per step at N=4096 on the host.
+same checks.  N=8192 (padded 12288^2, FP32 only: the cluster-split row passes
+and every other candidate), 3 steps against the FP64 oracle.  The oracle
+costs a few seconds per step at N=4096 and N=8192 on the host.
 """
 import math
 import os
@@ -155,3 +157,21 @@ def test_n2048_fp64_10_steps_vs_oracle(ts, run2048):
 def test_n2048_fp32_10_steps_vs_oracle(ts, run2048):
     errs = _check_fp32_all_candidates(ts, 2048, run2048)
     assert any("tma" in d for d in errs), errs
+
+
+@pytest.fixture(scope="module")
+def run8192(ts):
+    from palinstrophy_gb300 import _lib as L
+    if not L.supported(8192, "fp32"):
+        pytest.skip("fp32 is not compiled for N=8192")
+    return _oracle_run(8192, 3)
+
+
+def test_n8192_fp32_3_steps_vs_oracle(ts, run8192):
+    """The FP32 form at N=8192 against the FP64 oracle after 3 steps (NEXTDT
+    after step 1 replayed), for every row candidate -- the three cluster-split
+    row passes among them -- and every column candidate."""
+    errs = _check_fp32_all_candidates(ts, 8192, run8192)
+    assert max(errs.values()) <= 1e-5, errs
+    rows = {d.split(" col[")[0] for d in errs}
+    assert sum("cluster" in r for r in rows) == 3, rows

@@ -169,8 +169,11 @@ int pal_fp64_peak(double* tflops, double* ms);
  * pal_create times them on the new handle and keeps the fastest, once per
  * (precision, N) per process; PAL_AUTOTUNE=0 in the environment keeps the
  * first candidates instead, and PAL_TMA_MULTICAST=0 leaves out the candidates
- * that load by TMA cluster multicast (N=8192 "... mc ...").  pal_get_variant
- * reports the choice and a short
+ * that load by TMA cluster multicast (N=8192 "... mc ...").  With
+ * PAL_TUNE_FILE=<path>, a size listed in that file
+ * ("fp32 <N> <row name>|<column name>" per line) takes the named candidates
+ * without timing and a timed size is appended, so that later processes run
+ * the same kernels.  pal_get_variant reports the choice and a short
  * description; pal_set_variant forces one (between steps).  Performance
  * control; no counterpart in the reference. */
 int pal_get_variant(pal_handle* h, int* row, int* col, int* n_rows, int* n_cols, char* desc, size_t desc_len);

@@ -589,3 +589,40 @@ def test_multicast_candidates_can_be_left_out(ts):
                          env={**os.environ, "PAL_TMA_MULTICAST": "0"}, timeout=600)
     desc = out.stdout.strip().splitlines()[-1]
     assert desc.startswith("row[") and " mc " not in desc, desc
+
+
+def test_tuning_file_pins_the_candidates(ts, tmp_path):
+    """PAL_TUNE_FILE: a size listed there takes the named candidates without
+    timing, a size that is timed is appended, and a later process reading the
+    file runs the same kernels."""
+    import os
+    import subprocess
+    import sys
+    F = ts.Field(128, "fp32", 1e4, 0.5)
+    F.set_variant(1, 1)
+    want = F.variant()["desc"]
+    F.close()
+    rname = want.split("row[")[1].split("]")[0]
+    cname = want.split("col[")[1].split("]")[0]
+    tf = tmp_path / "tune.txt"
+    tf.write_text(f"# comment lines and other sizes are skipped\nfp64 128 {rname}|{cname}\nfp32 128 {rname}|{cname}\n")
+    code = ("from palinstrophy_gb300.turbo_simulator import Field\n"
+            "for n in (128, 64):\n"
+            "    F = Field(n, 'fp32', 1e4, 0.5)\n"
+            "    print(F.variant()['desc'])\n"
+            "    F.close()\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {**os.environ, "PAL_TUNE_FILE": str(tf)}
+    env.pop("PAL_AUTOTUNE", None)
+
+    def run():
+        out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, check=True,
+                             env=env, timeout=600)
+        return out.stdout.strip().splitlines()[-2:]
+
+    first = run()
+    assert first[0] == want
+    lines = tf.read_text().splitlines()
+    assert len(lines) == 4 and lines[3].startswith("fp32 64 "), lines
+    assert run() == first
+    assert len(tf.read_text().splitlines()) == 4  # nothing timed the second time

@@ -590,16 +590,17 @@ def _generator_times(N=N_GRID):
     return {"N": N, "spectrum": "KM3", "device_s": t_dev, "host_s": t_host}
 
 
-def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc):
+def _cpu_port_rate(steps_cap, seconds, workers, om2, uc, visc, warmup=1):
     """FP32 CPU port of the reference path (the oracle's FP32 mode, which is the
     reference's NumPy/scipy.fft step operation for operation, with the reference's
     elementwise passes on one thread as NumPy runs them): steps/s over a bounded
-    sample after one warm-up step."""
+    sample after `warmup` untimed steps."""
     import numpy as np
     from oracle import dns_oracle as do
     S = do.OracleState(N_GRID, om2, uc, visc, CFL, dtype=np.float32, workers=workers, threads=1)
     do.init_dt(S)
-    do.rk3(S)  # warm-up
+    for _ in range(warmup):
+        do.rk3(S)
     n, t0 = 0, time.perf_counter()
     while n < steps_cap and (time.perf_counter() - t0) < seconds:
         do.rk3(S)
@@ -706,13 +707,15 @@ def run_reference(args):
     from oracle import pao_generator as pg
     g = pg.generate_fast(N_GRID, K0, RE, SEED, "KM3")
     workers = min(8, os.cpu_count() or 1)
-    rate, n, secs = _cpu_port_rate(max(1, args.steps), 120.0, workers, g["om2"], g["uc_low"], float(g["visc"]))
-    sample = (f"{n} LS-IMEX-RK3 steps at N=4096 after 1 warm-up step ({secs:.1f} s), FP32 numpy/scipy.fft "
+    warmup = max(3, getattr(args, "warmup", 3))
+    rate, n, secs = _cpu_port_rate(max(1, args.steps), 120.0, workers, g["om2"], g["uc_low"], float(g["visc"]),
+                                   warmup=warmup)
+    sample = (f"{n} LS-IMEX-RK3 steps at N=4096 after {warmup} warm-up steps ({secs:.1f} s), FP32 numpy/scipy.fft "
               f"port of the reference path (oracle/dns_oracle.py), scipy.fft workers={workers} "
               f"(the reference's min(8, cores)), {os.cpu_count()} host cores, {_cpu_name()}")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": n, "warmup": 1, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
+        "steps": n, "warmup": warmup, "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (reference KM3 generator restated, seed 4895)",
         "config": {"workload": WORKLOAD.replace("FP32 form (FP64 dt/CFL/diagnostic scalars)",
                                                 "reference FP32 CPU path (numpy + scipy.fft)"), "N": N_GRID},

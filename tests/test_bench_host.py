@@ -59,7 +59,7 @@ def test_reference_arm_loads_nothing_from_the_product():
     (and its libpalgpu.so) is never imported."""
     code = (
         "import sys, types; sys.argv=['bench.py']; import bench; bench.N_GRID = 64; "
-        "bench.run_reference(types.SimpleNamespace(steps=2, gpus=1)); "
+        "bench.run_reference(types.SimpleNamespace(steps=2, warmup=3, gpus=1)); "
         "bad = [m for m in sys.modules if m.startswith('palinstrophy_gb300')]; "
         "assert not bad, bad; print('CLEAN')")
     out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)

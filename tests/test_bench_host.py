@@ -67,6 +67,7 @@ def test_reference_arm_loads_nothing_from_the_product():
     line = json.loads(out.stdout.strip().splitlines()[0])
     assert line["impl"] == "reference" and line["cpu_baseline"]["kind"] == "port"
     assert line["cpu_baseline"]["cores"] == min(8, os.cpu_count() or 1)
+    assert line["warmup"] >= 3 and "3 warm-up steps" in line["cpu_baseline"]["sample"]
     assert out.stdout.strip().endswith("CLEAN")
 
 

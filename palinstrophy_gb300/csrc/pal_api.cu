@@ -354,6 +354,8 @@ void tune_file_append(const pal_handle* h, int row, int col) {
 // The kernels' cost does not depend on the values they transform.
 int autotune(pal_handle* h) {
   const auto key = std::make_pair(h->precision, h->N);
+  // held while a size is timed: handles created concurrently wait for the one
+  // timing (once per size and process) instead of timing the same candidates
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   {
     auto it = g_tuned.find(key);

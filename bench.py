@@ -848,13 +848,29 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ncu-case", choices=["fp32", "fp64"], default=None,
-                    help="profiling target: init + 2 warm-up + 2 timed steps of one precision, no JSON")
+    ap.add_argument("--ncu-case", choices=["fp32", "fp64", "ensemble"], default=None,
+                    help="profiling target: init + 2 warm-up + 2 timed steps of one precision (or of the "
+                         "96-member ensemble, eager launches), no JSON")
     ap.add_argument("--ncu-n", type=int, default=N_GRID,
                     help="grid size of --ncu-case (4096 or 8192 FP32 / 4096 FP64), device generator start")
     ap.add_argument("--variant", default=None,
                     help="row,col kernel candidates for --ncu-case (skips the autotuning launches)")
     args = ap.parse_args()
+    if args.ncu_case == "ensemble":
+        from palinstrophy_gb300 import _lib as L
+        from palinstrophy_gb300.turbo_simulator import Ensemble
+        Ns = [256] * 32 + [384] * 32 + [512] * 32
+        E = Ensemble(Ns, "fp32", 1e4, 0.5)
+        for m, n in enumerate(Ns):
+            om2, uc, st = L.pao_generate(n, 10.0, 1e4, m + 1, "KM3")
+            E.set_member(m, om2, None, uc)
+            E.set_scalar(m, "visc", st["visc"])
+        E.init_dt()
+        E.step("CNAB2", 2, update=1, graph=False)
+        E.step("CNAB2", 2, update=1, graph=False)
+        E.synchronize()
+        E.close()
+        return
     if args.ncu_case:
         if args.variant:
             os.environ["PAL_AUTOTUNE"] = "0"

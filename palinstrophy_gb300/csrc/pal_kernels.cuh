@@ -182,6 +182,35 @@ __device__ __forceinline__ double block_max(double m, double* red, int tid) {
   return m;
 }
 
+// block_max and block_sum<NT, 1> of one value pair in one pass (one shared
+// round trip instead of two), with the same tree order as each of them.
+template <int NT>
+__device__ __forceinline__ void block_maxsum(double& m, double& s, double* red /* 2*NT/32 */, int tid) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    s += __shfl_xor_sync(0xffffffffu, s, off);
+  }
+  constexpr int NW = NT / 32;
+  if ((tid & 31) == 0) {
+    red[tid >> 5] = m;
+    red[NW + (tid >> 5)] = s;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    double mm = tid < NW ? red[tid] : 0.0;
+    double ss = tid < NW ? red[NW + tid] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      mm = fmax(mm, __shfl_xor_sync(0xffffffffu, mm, off));
+      ss += __shfl_xor_sync(0xffffffffu, ss, off);
+    }
+    m = mm;
+    s = ss;
+  }
+  __syncthreads();
+}
+
 // Compensated FP64 summation: s + c carries the running sum, c the exact
 // rounding errors of the additions into s (TwoSum, which needs no ordering of
 // the operands' magnitudes).
@@ -236,12 +265,15 @@ __device__ __forceinline__ void block_csum(double (&s)[K], double (&c)[K], doubl
 }
 
 // Returns true in every thread of the block that finished last of the nx
-// blocks counting on `counter`.
+// blocks counting on `counter`.  Whatever the last block reads of the others
+// (their partials) is written by their thread 0 before the call, so thread 0
+// alone fences before it takes its ticket; the CTA barrier before it orders
+// the rest of the block's work.
 __device__ __forceinline__ bool last_block(unsigned int* counter, int tid, int nx) {
   __shared__ int is_last;
-  __threadfence();
   __syncthreads();
   if (tid == 0) {
+    __threadfence();
     const unsigned int ticket = atomicAdd(counter, 1u);
     is_last = (ticket == (unsigned)nx - 1u);
   }
@@ -263,12 +295,13 @@ __device__ __forceinline__ bool last_block(unsigned int* counter, int tid) {
 template <int NT, bool COMP>
 __device__ void finish_stats(const StepArgs& a, double mx, double sum, double comp, int M, int tid, const Blk& bk) {
   __shared__ double red[2 * (NT / 32)];
-  mx = block_max<NT>(mx, red, tid);
   double s1[1] = {sum}, c1[1] = {comp};
-  if constexpr (COMP)
+  if constexpr (COMP) {
+    mx = block_max<NT>(mx, red, tid);
     block_csum<NT, 1>(s1, c1, red, tid);
-  else
-    block_sum<NT, 1>(s1, red, tid);
+  } else {
+    block_maxsum<NT>(mx, s1[0], red, tid);
+  }
   if (tid == 0) {
     a.part[2 * bk.x] = mx;
     a.part[2 * bk.x + 1] = s1[0];
@@ -284,11 +317,12 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, double co
     else
       s2[0] += __ldcg(a.part + 2 * q + 1);
   }
-  m2 = block_max<NT>(m2, red, tid);
-  if constexpr (COMP)
+  if constexpr (COMP) {
+    m2 = block_max<NT>(m2, red, tid);
     block_csum<NT, 1>(s2, c2, red, tid);
-  else
-    block_sum<NT, 1>(s2, red, tid);
+  } else {
+    block_maxsum<NT>(m2, s2[0], red, tid);
+  }
   if (tid == 0) {
     DevScalars* sc = a.sc;
     const double cflm = m2 * (double(a.N) / (2.0 * kPi));

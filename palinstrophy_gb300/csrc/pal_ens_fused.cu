@@ -31,14 +31,14 @@ struct FusedSize {
   static constexpr int V = VR;
   template <int NT>
   static __device__ __forceinline__ void row(const StepArgs& a, const TmaMaps& m, Blk bk) {
-    row_body<float, PLR, VR, NT, PFR>(a, m, bk);
+    row_body<float, PLR, VR, NT, PFR, true>(a, m, bk);
   }
   // QM: the flag-aware update of the RK3 stages that carry the combined term,
   // else the plain update (a separate launch, so CNAB2 passes keep the plain
   // body's register budget), as ColOf::col_perm chooses
   template <int NT, bool QM>
   static __device__ __forceinline__ void col(const StepArgs& a, Blk bk) {
-    col_body<float, PLC, NT, PREFC, true, QM>(a, bk);
+    col_body<float, PLC, NT, PREFC, true, QM, true>(a, bk);
   }
   template <int NT>
   static __device__ __forceinline__ void phys(const StepArgs& a, Blk bk) {

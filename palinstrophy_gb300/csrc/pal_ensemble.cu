@@ -6,7 +6,9 @@
 // so a step of the whole ensemble is 2 launches per group (CNAB2) or 6
 // (LS-IMEX-RK3) regardless of the member count.  Each member keeps its own
 // DevScalars: the fused CFL statistics in the row pass update that member's
-// dt, cn from its own CFLM, so per-member adaptive dt costs no extra launch.
+// dt, cn from its own CFLM, so per-member adaptive dt costs no extra launch
+// (in one-launch passes the row pass marks the member's max |u|+|v| and the
+// step's column passes form dt, cn from it: no last-block epilogue per row tile).
 // When every group's size belongs to a compiled fused set (pal_ens_fused.cu,
 // FP32), each pass is instead ONE launch over all groups -- 2 launches per
 // CNAB2 step, 6 per LS-IMEX-RK3 step, whatever the number of sizes -- with the
@@ -173,9 +175,13 @@ int om_layout(pal_ensemble* e, bool to_perm) {
 int launch_step(pal_ensemble* e, int method, bool dt_update) {
   const int stages = method == PAL_CNAB2 ? 1 : 3;
   for (int s = 0; s < stages; ++s) {
+    // one-launch passes (FP32): NEXTDT as a marked max in the row pass, formed
+    // by the step's column passes (F_STATS_MAX / F_DT_FROM_MAX); per-size
+    // launches: the row pass's own NEXTDT epilogue
+    const bool mark = e->fused != nullptr && dt_update;
     auto row_args = [&](const Group& g) {
       StepArgs a = group_args(e, g);
-      a.flags = (s == 0 && dt_update) ? (pal::F_STATS | pal::F_UPDATE_DT) : 0;
+      a.flags = (s == 0 && dt_update) ? (mark ? pal::F_STATS_MAX : (pal::F_STATS | pal::F_UPDATE_DT)) : 0;
       return a;
     };
     auto col_args = [&](const Group& g) {
@@ -186,7 +192,8 @@ int launch_step(pal_ensemble* e, int method, bool dt_update) {
         a.alpha = kRkAlpha[s];
         a.beta = kRkBeta[s];
       }
-      a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0);
+      a.flags = (s == stages - 1 ? pal::F_ADVANCE : 0) | (method == PAL_CNAB2 ? pal::F_CNM1 : 0) |
+                (mark ? pal::F_DT_FROM_MAX : 0);
       if (method != PAL_CNAB2) pal::rk3_stage_flags(a, s, kRkBeta);
       return a;
     };

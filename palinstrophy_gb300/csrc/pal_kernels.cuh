@@ -34,6 +34,16 @@ enum : int {
   F_Q_IN = 64,      // om holds q = (1 - K2 h1) om + c3 fnm1 of this stage; fnm1 is not read
   F_Q_OUT = 128,    // write the next stage's q (weights from beta_next) into om, not om and fn
   F_DIAG = 256,     // k_phys: the diagnostic sum of u^2+v^2, compensated FP64 (else a plain sum)
+  // FP32 row pass of a batched ensemble, NEXTDT every step: instead of the
+  // block reductions and the last-block epilogue of F_STATS, each warp folds
+  // its max |u|+|v| into DevScalars::step_max (an atomic max on the float's
+  // bits) and a non-finite sum into `nonfinite`; no barrier, fence or ticket.
+  F_STATS_MAX = 512,
+  // k_col: this step's dt and cn are the NEXTDT of step_max (as F_STATS |
+  // F_UPDATE_DT would have set them), formed by every block from the device
+  // scalars; the pass that ends the step (F_ADVANCE / F_CNM1) stores them,
+  // with CFLM and max |u|+|v|, and clears step_max.
+  F_DT_FROM_MAX = 1024,
 };
 
 // Device-resident scalars, FP64 in both precisions.
@@ -45,7 +55,8 @@ struct DevScalars {
   long long it;
   int nonfinite;
   int wait_timeout;  // set by a kernel whose bounded wait for its own bulk copies ran out
-  unsigned int row_counter, col_counter, diag_counter, phys_counter;
+  unsigned int row_counter, col_counter, diag_counter;
+  unsigned int step_max;  // F_STATS_MAX: bits of this step's max |u|+|v| (a float, >= 0)
 };
 
 struct StepArgs {
@@ -338,6 +349,40 @@ __device__ void finish_stats(const StepArgs& a, double mx, double sum, double co
     }
     sc->row_counter = 0u;
   }
+}
+
+// F_STATS_MAX epilogue of a row tile (FP32): the warp's max |u|+|v| into
+// step_max, a non-finite sum into `nonfinite`.  Non-negative floats order as
+// their bit patterns, so the atomic max of the bits is the max of the values,
+// whatever the order the warps arrive in.
+__device__ __forceinline__ void mark_step_max(const StepArgs& a, float mx, float acc, int tid) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  const bool bad = __any_sync(0xffffffffu, !isfinite(acc));
+  if ((tid & 31) == 0) {
+    atomicMax(&a.sc->step_max, __float_as_uint(mx));
+    if (bad) atomicOr(&a.sc->nonfinite, 1);
+  }
+}
+
+// NEXTDT from step_max (F_DT_FROM_MAX), the same arithmetic as finish_stats's
+// last block: the step's dt and cn, CFLM and max |u|+|v|.
+struct NextDt {
+  double dt, cn, cflm, maxabs;
+};
+__device__ __forceinline__ NextDt nextdt_from_mark(const StepArgs& a) {
+  const DevScalars* sc = a.sc;
+  NextDt r;
+  r.maxabs = double(__uint_as_float(sc->step_max));
+  r.cflm = r.maxabs * (double(a.N) / (2.0 * kPi));
+  r.dt = sc->dt;
+  r.cn = sc->cn;
+  if (r.cflm > 0.0 && sc->dt > 0.0) {
+    const double cfl = r.cflm * sc->dt * kPi;
+    r.cn = 0.8 + 0.2 * (sc->cflnum / cfl);
+    r.dt = sc->dt * r.cn;
+  }
+  return r;
 }
 
 // --------------------------------------------------------------------------
@@ -822,7 +867,8 @@ constexpr int row_tiles_per_sm() {
   // block's static shared memory (mbarrier, reduction scratch)
   return int(size_t(228 * 1024) / (size_t(PL::PADM) * V * sizeof(cplx<T>) + 1024 + 256));
 }
-template <typename T, class PL, int V, int NT, int PF>
+// ENS: the ensemble's one-launch row pass, which honours F_STATS_MAX.
+template <typename T, class PL, int V, int NT, int PF, bool ENS = false>
 __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps, const Blk bk) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C), bk.y);
@@ -853,7 +899,7 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
     row_first_pass<T, PL, V, NT>(a, sm, z0, tid);
   }
   dif_range<T, PL, V, NT, +1, 1, PL::NP - 1>(sm, tw, tid);
-  const bool stats = (a.flags & F_STATS) != 0;
+  const bool stats = (a.flags & (ENS ? (F_STATS | F_STATS_MAX) : F_STATS)) != 0;
   T mx = T(0), acc = T(0);
   row_products<T, PL, V, NT>(sm, tid, stats, mx, acc);
   if constexpr (sizeof(C) == 8) {
@@ -877,7 +923,14 @@ __device__ __forceinline__ void row_body(const StepArgs& a0, const TmaMaps& maps
       w1[(size_t)k * M + z0 + v] = C{T(0.5) * (p.y + q.y), T(-0.5) * (p.x - q.x)};
     }
   }
-  if (stats) finish_stats<NT, false>(a, double(mx), double(acc), 0.0, M, tid, bk);
+  if constexpr (ENS && sizeof(T) == 4) {
+    if (a.flags & F_STATS)
+      finish_stats<NT, false>(a, double(mx), double(acc), 0.0, M, tid, bk);
+    else if (a.flags & F_STATS_MAX)
+      mark_step_max(a, mx, acc, tid);
+  } else {
+    if (stats) finish_stats<NT, false>(a, double(mx), double(acc), 0.0, M, tid, bk);
+  }
 }
 template <typename T, class PL, int V, int NT, int PF>
 __global__ void __launch_bounds__(NT, (PF & 16) ? row_tiles_per_sm<T, PL, V>() : 0)
@@ -950,11 +1003,16 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // Implicit / explicit weights of the column update, formed in FP64 from the
 // device scalars: CNAB2 (turbo_simulator.py:1745-1752) or one RK3 stage.
-template <typename T>
+// ENS: the ensemble's one-launch column pass, which honours F_DT_FROM_MAX.
+template <typename T, bool ENS = false>
 __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
   ModeCoef<T> cf;
   const DevScalars* sc = a.sc;
-  const double dt = sc->dt, visc = sc->visc;
+  double dt = sc->dt;
+  if constexpr (ENS) {
+    if (a.flags & F_DT_FROM_MAX) dt = nextdt_from_mark(a).dt;
+  }
+  const double visc = sc->visc;
   double h1, h2, c2, c3;
   if (a.scheme == 0) {
     const double cnm1 = sc->cnm1;
@@ -976,6 +1034,18 @@ __device__ __forceinline__ ModeCoef<T> col_coef(const StepArgs& a, int N) {
   const T m32 = T(1.5) * T(N);
   cf.divxz = T(1) / (m32 * m32);
   return cf;
+}
+
+// The coefficients formed once per block: col_coef's FP64 arithmetic (and the
+// FP64 division of F_DT_FROM_MAX) is uniform across the block, and FP64 issue
+// is scarce, so warp 0 alone forms them and thread 0 leaves them in shared
+// memory; the block reads them after its next barrier.
+template <typename T, bool ENS>
+__device__ __forceinline__ void col_coef_shared(const StepArgs& a, int N, int tid, ModeCoef<T>* s) {
+  if (tid < 32) {
+    const ModeCoef<T> c = col_coef<T, ENS>(a, N);
+    if (tid == 0) *s = c;
+  }
 }
 
 // Planar column tile for bulk tensor copies: plane v (A / u^, B / v^) starts at
@@ -1189,11 +1259,21 @@ __device__ __forceinline__ void col_last_pass(const cplx<T>* sm, cplx<T>* __rest
 }
 
 // Time / cnm1 bookkeeping of the step, done once by the last block to finish.
-template <int NT>
+template <int NT, bool ENS = false>
 __device__ __forceinline__ void col_finish(const StepArgs& a, int tid, int nx) {
   if (a.flags & (F_ADVANCE | F_CNM1)) {
     if (last_block(&a.sc->col_counter, tid, nx) && tid == 0) {
       DevScalars* sc = a.sc;
+      if constexpr (ENS) {
+        if (a.flags & F_DT_FROM_MAX) {  // every block has read the old dt, cn and step_max
+          const NextDt nd = nextdt_from_mark(a);
+          sc->maxabs = nd.maxabs;
+          sc->cflm = nd.cflm;
+          sc->dt = nd.dt;
+          sc->cn = nd.cn;
+          sc->step_max = 0u;
+        }
+      }
       if (a.flags & F_ADVANCE) {
         sc->t += sc->dt;
         sc->it += 1;
@@ -1211,7 +1291,10 @@ __device__ __forceinline__ void col_finish(const StepArgs& a, int tid, int nx) {
 // also overlaps the pass-0 loads of a thread's next butterfly.  With
 // PERM the kernel works on om_p / fm_p (butterfly-major columns of M elements).
 // QM: the RK3 stage flags F_Q_IN / F_Q_OUT / F_NO_FM_IN are honoured (col_middle).
-template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true>
+// ENS: the ensemble's one-launch pass: F_DT_FROM_MAX honoured, and the FP64
+// coefficients formed once per block (col_coef_shared), which pays with the
+// ensemble's many small column blocks.
+template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true, bool ENS = false>
 __device__ __forceinline__ void col_body(const StepArgs& a0, const Blk bk) {
   using C = cplx<T>;
   const StepArgs a = member_args(a0, sizeof(C), bk.y);
@@ -1239,7 +1322,12 @@ __device__ __forceinline__ void col_body(const StepArgs& a0, const Blk bk) {
     }
     cp_async_commit();
   }
-  const ModeCoef<T> cf = col_coef<T>(a, N);
+  __shared__ ModeCoef<T> s_cf;
+  ModeCoef<T> cf0;
+  if constexpr (ENS)
+    col_coef_shared<T, true>(a, N, tid, &s_cf);  // read after the barriers of pass 0
+  else
+    cf0 = col_coef<T>(a, N);
 
   // pass 0 (forward z-DIF) straight from the P planes.  PREF == 3: the loads
   // of a thread's next butterfly are issued before the current one's DFT.
@@ -1297,11 +1385,12 @@ __device__ __forceinline__ void col_body(const StepArgs& a0, const Blk bk) {
     cp_async_wait_all();
     __syncthreads();
   }
+  const ModeCoef<T> cf = ENS ? s_cf : cf0;
   col_middle<T, PL, NT, PREF == 1 && !PERM, PERM, PREF == 2 || PREF == 3, QM>(sm, s_om, s_fm, om, fm, cf, kx,
                                                                              tid, a.flags);
   dit_range<T, PL, V, NT, +1, PL::NP - 2, 1>(sm, tw, tid);
   col_last_pass<T, PL, NT>(sm, w0, w1, tw, kx, tid);
-  col_finish<NT>(a, tid, bk.nx);
+  col_finish<NT, ENS>(a, tid, bk.nx);
 }
 template <typename T, class PL, int NT, int PREF, bool PERM, bool QM = true>
 __global__ void __launch_bounds__(NT) k_col(StepArgs a0) {
@@ -1477,6 +1566,8 @@ __global__ void __launch_bounds__(NT, MINB) k_col_tma(StepArgs a0, const __grid_
       tma_load_3d(&maps.w1, sm + CP::PB + g * (CP::RP + 2), &bar, 0, g, row);
     }
   }
+  // every thread forms the coefficients while the bulk copies are in flight
+  // (one warp forming them for the block measured 2 % slower here)
   const ModeCoef<T> cf = col_coef<T>(a, N);
   __syncthreads();  // every thread sees the initialised barrier
   if (!mbar_test_wait(&bar, 0, a.dbg_wait0 ? 0 : 1 << 20)) {
